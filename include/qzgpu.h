@@ -1,0 +1,142 @@
+/*
+ * qzgpu — GB300 (sm_103a) block sorting for qz's BSC stage.
+ *
+ * C ABI only: plain pointers and sizes, no CUDA or torch types.  The entry
+ * points below replace the block-sorting stage that qz reaches through
+ * libbsc (crates/qz-lib/src/compression/bsc.rs:91-125):
+ *
+ *   - the forward BWT that bsc_compress runs on each block
+ *     (called at bsc.rs:172-183 with blockSorter = LIBBSC_BLOCKSORTER_BWT);
+ *   - the inverse BWT that bsc_decompress runs after the QLFC decoder
+ *     (called at bsc.rs:421-433).
+ *
+ * libbsc's own BWT hooks (bsc_bwt_encode / bsc_bwt_decode in libbsc/bwt/bwt.h)
+ * are not in the reference tree (third_party/ is git-ignored, .gitignore:31);
+ * qzgpu_bwt_encode / qzgpu_bwt_decode keep their argument meaning: the block
+ * is transformed in place in a caller-owned host buffer, the forward call
+ * returns the primary index, and errors are libbsc's negative codes.
+ *
+ * Output convention (libsais, libbsc's CPU sorter): U[0] = T[n-1], followed by
+ * the last column of the sorted suffix matrix with the sentinel row dropped;
+ * primary index = 1 + rank of the whole block among its n non-empty suffixes.
+ * Auxiliary index k (sampling rate r, a power of two) = 1 + rank of suffix k*r.
+ *
+ * Thread safety: every entry point may be called concurrently from many host
+ * threads (qz calls the BSC wrapper from rayon workers, bsc.rs:285-288).
+ */
+#ifndef QZGPU_H
+#define QZGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error codes: 0 and -1..-6 are libbsc's (bsc.rs:17-24); -7.. are GPU-side. */
+#define QZGPU_NO_ERROR 0
+#define QZGPU_BAD_PARAMETER (-1)
+#define QZGPU_NOT_ENOUGH_MEMORY (-2)
+#define QZGPU_NOT_COMPRESSIBLE (-3)
+#define QZGPU_NOT_SUPPORTED (-4)
+#define QZGPU_UNEXPECTED_EOB (-5)
+#define QZGPU_DATA_CORRUPT (-6)
+#define QZGPU_GPU_ERROR (-7)
+#define QZGPU_GPU_NOT_SUPPORTED (-8)
+#define QZGPU_GPU_NOT_ENOUGH_MEMORY (-9)
+#define QZGPU_TIMEOUT (-10)
+
+/* libbsc feature bits (bsc.rs:32-36).  Accepted for signature compatibility;
+ * the GPU path is always taken and never falls back to the CPU. */
+#define QZGPU_FEATURE_FASTMODE 1
+#define QZGPU_FEATURE_MULTITHREADING 2
+#define QZGPU_FEATURE_LARGEPAGES 4
+#define QZGPU_FEATURE_CUDA 8
+
+/* Largest block one call accepts (libbsc's c_int limit, bsc.rs:165-167), and
+ * the largest total of one device batch (keeps all positions in int32). */
+#define QZGPU_MAX_BLOCK (1 << 30)
+#define QZGPU_MAX_BATCH_BYTES (1LL << 30)
+
+/* One-time initialisation; replaces bsc_init (bsc.rs:93, called once through
+ * std::sync::Once at bsc.rs:128-141).  Selects the current CUDA device and
+ * creates the shared scratch pool.  Idempotent; returns 0 or a negative code. */
+int qzgpu_init(int features);
+
+/* Human-readable name of an error code (never NULL). */
+const char *qzgpu_error_string(int code);
+
+/* ------------------------------------------------------------------------- */
+/* libbsc BWT-stage drop-ins (host buffers, block transformed in place).       */
+/* ------------------------------------------------------------------------- */
+
+/* Forward BWT of T[0..n) in place; replaces libbsc's bsc_bwt_encode, which
+ * bsc_compress runs for blockSorter = BWT (bsc.rs:172-183).  Returns the
+ * primary index (>= 1; n for n <= 1) or a negative error.  When indexes is not
+ * NULL, *num_indexes receives the auxiliary index count for rate
+ * qzgpu_aux_rate(n) and indexes[0..*num_indexes) the indexes of suffixes
+ * r, 2r, ... (indexes must hold 256 entries). */
+int qzgpu_bwt_encode(unsigned char *T, int n, unsigned char *num_indexes, int *indexes, int features);
+
+/* Inverse BWT of T[0..n) in place given the primary index; replaces libbsc's
+ * bsc_bwt_decode, which bsc_decompress runs after QLFC decoding
+ * (bsc.rs:421-433).  Auxiliary indexes are optional (num_indexes may be 0).
+ * Returns 0, QZGPU_DATA_CORRUPT for an index or BWT that cannot be inverted,
+ * or another negative code. */
+int qzgpu_bwt_decode(unsigned char *T, int n, int index, unsigned char num_indexes, const int *indexes,
+                     int features);
+
+/* Auxiliary-index sampling rate used by qzgpu_bwt_encode for a block of n
+ * bytes: the largest power of two <= max(n / 8, 1). */
+int qzgpu_aux_rate(int n);
+
+/* ------------------------------------------------------------------------- */
+/* Device scratch storage (libcubwt-style: allocate once, reuse per call).     */
+/* ------------------------------------------------------------------------- */
+
+typedef struct qzgpu_storage qzgpu_storage;
+
+/* Allocates device scratch for batches of up to max_total_bytes block bytes
+ * and max_blocks blocks (about 60 bytes of HBM per block byte). */
+int qzgpu_storage_create(qzgpu_storage **storage, long long max_total_bytes, int max_blocks);
+int qzgpu_storage_destroy(qzgpu_storage *storage);
+
+/* Device bytes one storage of this capacity allocates (for admission). */
+long long qzgpu_storage_bytes(long long max_total_bytes, int max_blocks);
+
+/* ------------------------------------------------------------------------- */
+/* Batched forms: many blocks of uneven size in one set of launches.          */
+/* ------------------------------------------------------------------------- */
+
+/* Host buffers: forward BWT of blocks T[b][0..n[b]) into U[b] (U may equal T);
+ * indexes[b] receives each primary index.  Replaces a rayon fan-out of
+ * bsc_compress calls (compress_parallel_with, bsc.rs:259-301). */
+int qzgpu_bwt_encode_batch(qzgpu_storage *storage, int nblocks, const unsigned char *const *T,
+                           unsigned char *const *U, const int *n, int *indexes, int features);
+
+/* Host buffers: inverse BWT of U[b] into T[b] (may alias).  Replaces the
+ * parallel bsc_decompress fan-out of decompress_parallel (bsc.rs:324-371). */
+int qzgpu_bwt_decode_batch(qzgpu_storage *storage, int nblocks, const unsigned char *const *U,
+                           unsigned char *const *T, const int *n, const int *indexes, int features);
+
+/* Device-resident form.  d_T / d_U hold the blocks back to back (block b at
+ * offset n[0]+...+n[b-1]); n[] and indexes[] are host arrays.  Work is issued
+ * on `stream` (a cudaStream_t, NULL for the legacy default stream); the call
+ * returns once the results are final. */
+int qzgpu_bwt_encode_device(qzgpu_storage *storage, int nblocks, const int *n, const unsigned char *d_T,
+                            unsigned char *d_U, int *indexes, void *stream);
+int qzgpu_bwt_decode_device(qzgpu_storage *storage, int nblocks, const int *n, const int *indexes,
+                            const unsigned char *d_U, unsigned char *d_T, void *stream);
+
+/* Counters from the last forward call on a storage. */
+typedef struct qzgpu_stats {
+    int rounds;               /* prefix-doubling rounds after the initial sort */
+    int kernel_launches;      /* kernels this library launched for the call */
+    long long active_total;   /* sum over rounds of suffixes still unsorted */
+    long long alg_bytes;      /* algorithmic HBM bytes of the call */
+} qzgpu_stats;
+int qzgpu_storage_last_stats(const qzgpu_storage *storage, qzgpu_stats *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QZGPU_H */

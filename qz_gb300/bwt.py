@@ -1,0 +1,155 @@
+"""Python host API over the C ABI: the calls qz's BSC wrapper makes, one block
+or many, on host or device buffers.
+
+Mirrors the block surface of crates/qz-lib/src/compression/bsc.rs: empty input
+short-circuits before the library is called (bsc.rs:162-164, 387-389), sizes
+above c_int::MAX are rejected (bsc.rs:165-167), and any negative library code
+raises (bsc.rs:185-187, 411-433 turn them into anyhow errors).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import native
+from .native import QzGpuError, check
+
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+C_INT_MAX = 2**31 - 1
+
+
+def _as_u8(data) -> np.ndarray:
+    if isinstance(data, (bytes, bytearray, memoryview)):
+        return np.frombuffer(bytes(data), dtype=np.uint8).copy()
+    return np.array(data, dtype=np.uint8, copy=True)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_u8p)
+
+
+def init() -> None:
+    check(native.load().qzgpu_init(0), "qzgpu_init")
+
+
+def aux_rate(n: int) -> int:
+    return native.load().qzgpu_aux_rate(int(n))
+
+
+def bwt_encode(data, with_aux: bool = False):
+    """Forward BWT of one block (libbsc's bsc_bwt_encode semantics).
+
+    Returns (U, primary_index) or (U, primary_index, aux_indexes)."""
+    t = _as_u8(data)
+    n = len(t)
+    if n > C_INT_MAX:
+        raise QzGpuError(native.QZGPU_BAD_PARAMETER, f"BSC input too large: {n} bytes")
+    L = native.load()
+    num = ctypes.c_uint8(0)
+    aux = np.zeros(256, dtype=np.int32)
+    buf = t if n else np.zeros(1, np.uint8)
+    rc = L.qzgpu_bwt_encode(_ptr(buf), n, ctypes.cast(ctypes.pointer(num), _u8p) if with_aux else None,
+                            aux.ctypes.data_as(_i32p) if with_aux else None, 0)
+    check(rc, "qzgpu_bwt_encode")
+    if with_aux:
+        return t, rc, aux[: num.value].copy()
+    return t, rc
+
+
+def bwt_decode(u, index: int) -> np.ndarray:
+    """Inverse BWT of one block (libbsc's bsc_bwt_decode semantics)."""
+    t = _as_u8(u)
+    n = len(t)
+    buf = t if n else np.zeros(1, np.uint8)
+    check(native.load().qzgpu_bwt_decode(_ptr(buf), n, int(index), 0, None, 0), "qzgpu_bwt_decode")
+    return t
+
+
+class Storage:
+    """Device scratch for batches of up to ``max_total_bytes`` bytes in
+    ``max_blocks`` blocks (libcubwt-style: allocate once, reuse)."""
+
+    def __init__(self, max_total_bytes: int, max_blocks: int = 1):
+        self._lib = native.load()
+        h = ctypes.c_void_p()
+        check(self._lib.qzgpu_storage_create(ctypes.byref(h), int(max_total_bytes), int(max_blocks)),
+              "qzgpu_storage_create")
+        self._h = h
+        self.max_total_bytes = int(max_total_bytes)
+        self.max_blocks = int(max_blocks)
+
+    @staticmethod
+    def device_bytes(max_total_bytes: int, max_blocks: int) -> int:
+        return native.load().qzgpu_storage_bytes(int(max_total_bytes), int(max_blocks))
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.qzgpu_storage_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def stats(self) -> dict:
+        s = native.Stats()
+        check(self._lib.qzgpu_storage_last_stats(self._h, ctypes.byref(s)), "qzgpu_storage_last_stats")
+        return {"rounds": s.rounds, "kernel_launches": s.kernel_launches, "active_total": s.active_total,
+                "alg_bytes": s.alg_bytes}
+
+    def _ptr_arrays(self, ins, outs):
+        nb = len(ins)
+        inp = (_u8p * max(nb, 1))(*[_ptr(b) for b in ins])
+        outp = (_u8p * max(nb, 1))(*[_ptr(b) for b in outs])
+        return inp, outp
+
+    def encode_batch(self, blocks):
+        """Forward BWT of many blocks in one batched launch sequence.
+        Returns (list of U, list of primary indexes)."""
+        ins = [_as_u8(b) for b in blocks]
+        ins = [b if len(b) else np.zeros(1, np.uint8) for b in ins]
+        sizes = np.array([len(b) for b in blocks] or [0], dtype=np.int32)
+        outs = [np.empty(max(len(b), 1), np.uint8) for b in ins]
+        idx = np.zeros(max(len(blocks), 1), dtype=np.int32)
+        inp, outp = self._ptr_arrays(ins, outs)
+        check(self._lib.qzgpu_bwt_encode_batch(self._h, len(blocks), inp, outp, sizes.ctypes.data_as(_i32p),
+                                               idx.ctypes.data_as(_i32p), 0), "qzgpu_bwt_encode_batch")
+        return [o[: s] for o, s in zip(outs, sizes)], [int(i) for i in idx[: len(blocks)]]
+
+    def decode_batch(self, blocks, indexes):
+        ins = [_as_u8(b) for b in blocks]
+        ins = [b if len(b) else np.zeros(1, np.uint8) for b in ins]
+        sizes = np.array([len(b) for b in blocks] or [0], dtype=np.int32)
+        outs = [np.empty(max(len(b), 1), np.uint8) for b in ins]
+        idx = np.array(list(indexes) or [0], dtype=np.int32)
+        inp, outp = self._ptr_arrays(ins, outs)
+        check(self._lib.qzgpu_bwt_decode_batch(self._h, len(blocks), inp, outp, sizes.ctypes.data_as(_i32p),
+                                               idx.ctypes.data_as(_i32p), 0), "qzgpu_bwt_decode_batch")
+        return [o[: s] for o, s in zip(outs, sizes)]
+
+    def encode_device(self, sizes, d_T: int, d_U: int, stream: int = 0):
+        """Device buffers (blocks back to back) -> list of primary indexes."""
+        sz = np.array(list(sizes) or [0], dtype=np.int32)
+        idx = np.zeros(max(len(sizes), 1), dtype=np.int32)
+        check(self._lib.qzgpu_bwt_encode_device(self._h, len(sizes), sz.ctypes.data_as(_i32p), ctypes.c_void_p(d_T),
+                                                ctypes.c_void_p(d_U), idx.ctypes.data_as(_i32p),
+                                                ctypes.c_void_p(stream)), "qzgpu_bwt_encode_device")
+        return [int(i) for i in idx[: len(sizes)]]
+
+    def decode_device(self, sizes, indexes, d_U: int, d_T: int, stream: int = 0) -> None:
+        sz = np.array(list(sizes) or [0], dtype=np.int32)
+        idx = np.array(list(indexes) or [0], dtype=np.int32)
+        check(self._lib.qzgpu_bwt_decode_device(self._h, len(sizes), sz.ctypes.data_as(_i32p),
+                                                idx.ctypes.data_as(_i32p), ctypes.c_void_p(d_U),
+                                                ctypes.c_void_p(d_T), ctypes.c_void_p(stream)),
+              "qzgpu_bwt_decode_device")

@@ -1,0 +1,119 @@
+// Shared device helpers for the block-sorting kernels (sm_103a).
+// Integer-only code: warp shuffles and shared-memory scans, no tensor cores.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/qzgpu.h"
+
+namespace qz {
+
+constexpr int kThreads = 256;  // threads per CTA for the streaming kernels
+constexpr int kWarps = kThreads / 32;
+
+// Device status word: kernels never trap; they record the first problem here
+// and return, and the host turns it into a QZGPU_* error code.
+struct DevStatus {
+    int error;   // QZGPU_* code, 0 if fine
+    int where;   // kernel tag
+    long long detail;
+};
+
+__device__ __forceinline__ void report(DevStatus* st, int code, int where, long long detail) {
+    if (atomicCAS(&st->error, 0, code) == 0) {
+        st->where = where;
+        st->detail = detail;
+    }
+}
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ unsigned warp_id() { return threadIdx.x >> 5; }
+
+template <typename T>
+__device__ __forceinline__ T warp_incl_sum(T v) {
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        T t = __shfl_up_sync(0xffffffffu, v, d);
+        if ((int)lane_id() >= d) v += t;
+    }
+    return v;
+}
+
+__device__ __forceinline__ int warp_incl_max(int v) {
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, v, d);
+        if ((int)lane_id() >= d) v = max(v, t);
+    }
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+    return v;
+}
+
+// Block-wide exclusive sum over kThreads threads. `sh` needs kWarps+1 slots.
+// Returns the exclusive prefix for this thread; *total receives the sum.
+template <typename T>
+__device__ __forceinline__ T block_excl_sum(T v, T* sh, T* total) {
+    T inc = warp_incl_sum(v);
+    if (lane_id() == 31) sh[warp_id()] = inc;
+    __syncthreads();
+    if (warp_id() == 0) {
+        T w = lane_id() < (unsigned)kWarps ? sh[lane_id()] : T(0);
+        T wi = warp_incl_sum(w);
+        if (lane_id() < (unsigned)kWarps) sh[lane_id()] = wi - w;
+        if (lane_id() == (unsigned)kWarps - 1) sh[kWarps] = wi;
+    }
+    __syncthreads();
+    T res = sh[warp_id()] + inc - v;
+    *total = sh[kWarps];
+    __syncthreads();
+    return res;
+}
+
+// Block-wide inclusive max over kThreads threads. `sh` needs kWarps+1 slots.
+__device__ __forceinline__ int block_incl_max(int v, int* sh, int* total) {
+    int inc = warp_incl_max(v);
+    if (lane_id() == 31) sh[warp_id()] = inc;
+    __syncthreads();
+    if (warp_id() == 0) {
+        int w = lane_id() < (unsigned)kWarps ? sh[lane_id()] : INT32_MIN;
+        int wi = warp_incl_max(w);
+        int ex = __shfl_up_sync(0xffffffffu, wi, 1);
+        if (lane_id() == 0) ex = INT32_MIN;
+        if (lane_id() < (unsigned)kWarps) sh[lane_id()] = ex;
+        if (lane_id() == (unsigned)kWarps - 1) sh[kWarps] = wi;
+    }
+    __syncthreads();
+    int res = max(sh[warp_id()], inc);
+    *total = sh[kWarps];
+    __syncthreads();
+    return res;
+}
+
+// Index of the block that owns global position x: off[b] <= x < off[b+1].
+__device__ __forceinline__ int block_of(const int* __restrict__ off, int nblocks, int x) {
+    int lo = 0, hi = nblocks - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(off + mid) <= x) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Chunk of [0, len) owned by CTA `c` of `grid`, rounded to `align` elements.
+__device__ __forceinline__ void chunk_range(int len, int grid, int c, int align, int* lo, int* hi) {
+    long long per = ((long long)len + grid - 1) / grid;
+    per = (per + align - 1) / align * align;
+    long long a = per * c, b = a + per;
+    if (a > len) a = len;
+    if (b > len) b = len;
+    *lo = (int)a;
+    *hi = (int)b;
+}
+
+}  // namespace qz

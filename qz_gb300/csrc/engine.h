@@ -1,0 +1,126 @@
+// Host-side engine for the block-sorting kernels: device scratch layout of one
+// storage, and the forward / inverse drivers the C ABI (qzgpu.cu) wraps.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+
+namespace qz {
+
+// Segment classes of the per-round sort (by group length).
+constexpr int kSmallMax = 16;    // one thread, register bitonic network
+constexpr int kMedMax = 4096;    // one CTA, shared-memory bitonic sort
+constexpr int kRT = 4096;        // tile of the segmented radix sort (larger groups)
+constexpr int kInitTile = 4096;  // text positions per tile of the per-block passes
+constexpr int kSplitGrid = 1024; // fixed grid of the split phases
+constexpr int kMaxRounds = 40;   // prefix doubling needs <= 31 rounds for n < 2^31
+
+// Device counters (int32 slots of Storage::counters).
+enum Counter {
+    CNT_ACTIVE = 0,  // suffixes still in non-singleton groups
+    CNT_SMALL = 1,   // descriptor counts per class
+    CNT_MED = 2,
+    CNT_LARGE = 3,
+    CNT_LTILES = 4,  // tiles of the large-group radix sort
+    CNT_LHIST = 5,   // histogram entries of the large-group radix sort (256 per tile)
+    CNT_SLOTS = 16,
+};
+
+struct FwdBuffers {
+    int* SA;
+    int* R;
+    uint32_t* key;
+    int* W[2];
+    int* P[2];
+    int* G[2];
+    uint32_t* wsk[2];
+    int* wsv[2];
+    int2* list[3];
+    uint32_t* ltc;     // large: tiles per segment -> tile base
+    uint32_t* llen;    // large: length per segment -> workspace base
+    uint32_t* ltbase;
+    uint32_t* lwbase;
+};
+
+struct InvBuffers {
+    int* LF;
+    int* rnext[2];
+    int* rdist[2];
+    int* rlen;
+    int* rrow;      // ruler -> block (for the jump kernel)
+    int2* rtiles;   // (block, first ruler) per walk tile
+};
+
+struct Storage {
+    long long cap_bytes = 0;
+    int cap_blocks = 0;
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;  // internal stream for host-buffer calls
+
+    // one device allocation, carved into the forward and inverse layouts
+    char* dev = nullptr;
+    size_t dev_bytes = 0;
+
+    uint8_t* T = nullptr;  // staging copies for host-buffer calls
+    uint8_t* U = nullptr;
+    uint32_t* hist = nullptr;     // per-tile digit histograms (large sort / LF build)
+    size_t hist_cap = 0;          // uint32 entries
+    uint32_t* partial = nullptr;  // scan partials
+    int* split_part = nullptr;    // split phase partials (2 * kSplitGrid)
+    int* counters = nullptr;
+    DevStatus* status = nullptr;
+
+    // per-block tables
+    int* blk_off = nullptr;     // nb + 1
+    int* blk_K = nullptr;       // initial sort depth
+    int* blk_sigma = nullptr;
+    uint8_t* blk_code = nullptr;  // nb * 256 dense symbol codes
+    uint32_t* blk_hist = nullptr; // nb * 256 byte counts
+    int* blk_idx = nullptr;       // primary indexes out
+    int* blk_aux_rate = nullptr;
+    int* blk_aux_off = nullptr;
+    int* aux = nullptr;           // auxiliary indexes out
+    int2* tiles = nullptr;        // (block, start) per kInitTile tile
+    int* blk_tbase = nullptr;     // first tile of each block
+
+    FwdBuffers f{};
+    InvBuffers v{};
+
+    // pinned host staging
+    char* pin = nullptr;
+    size_t pin_bytes = 0;
+    uint8_t* pin_T = nullptr;  // host-buffer calls: input staging
+    uint8_t* pin_U = nullptr;  // host-buffer calls: output staging
+    char* pin_tab = nullptr;   // tables
+    int* pin_rd = nullptr;     // small device->host readbacks
+    size_t pin_tab_bytes = 0;
+
+    std::mutex mu;
+    qzgpu_stats stats{};
+    std::vector<int> rounds_active;  // active suffixes per round of the last forward call
+};
+
+size_t storage_device_bytes(long long cap_bytes, int cap_blocks);
+int storage_init(Storage* S, long long cap_bytes, int cap_blocks);
+void storage_free(Storage* S);
+
+// Forward BWT of nb blocks laid out back to back in d_T (device).  n: host
+// sizes.  idx (host, nb) receives primary indexes; aux_rate (host, may be
+// null) selects per-block auxiliary index rates and aux_out (host, may be
+// null) receives (n-1)/rate indexes per block, back to back.
+int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d_U, int* idx,
+                const int* aux_rate, int* aux_out, cudaStream_t st);
+
+// Inverse BWT of nb blocks (d_U back to back, device) into d_T.
+int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t* d_U, uint8_t* d_T,
+                cudaStream_t st);
+
+int map_cuda_error(cudaError_t e);
+
+}  // namespace qz

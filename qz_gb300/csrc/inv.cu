@@ -1,0 +1,318 @@
+// Inverse BWT of a batch of blocks by LF-mapping on sm_103a.
+//
+// Replaces the inverse transform libbsc runs inside bsc_decompress after QLFC
+// decoding (reached from crates/qz-lib/src/compression/bsc.rs:421-433).
+//
+// Block b has n_b + 1 rows (row 0 = the empty suffix, row p_b = the whole
+// block, whose last-column symbol is the dropped sentinel).  Rows of all
+// blocks are stored back to back: block b's rows start at off[b] + b.
+//
+//   1. LF build: a stable ranking of U by symbol per block (per-tile 8-bit
+//      histograms, one device-wide scan, warp match-based ranks), so
+//      LF[row] = 1 + (number of symbols < c) + (occurrences of c before row);
+//   2. list ranking of the single LF cycle: rows r with r % stride == 0 are
+//      rulers; each ruler walks LF to the next ruler (walk 1), ruler
+//      distances to row 0 come from pointer jumping, and each ruler walks its
+//      stretch again writing T[n - d] = F(row) (walk 2), F read from the
+//      block's symbol start table in shared memory.
+// Every row is read twice; every wait is a bounded loop and a broken LF cycle
+// (corrupt input) is reported as QZGPU_DATA_CORRUPT.
+#include <algorithm>
+
+#include "engine.h"
+#include "scan.cuh"
+
+namespace qz {
+
+constexpr int kIRItems = kInitTile / kThreads;  // 16
+constexpr int kIRWarpSpan = kInitTile / kWarps;  // 512
+
+struct InvArgs {
+    const uint8_t* U;
+    const int* off;
+    const int* idx;
+    const int* tbase;  // first histogram tile of each block
+    const int* rbase;  // first ruler of each block
+    const int2* tiles; // (block, start) per kInitTile tile of U
+    int* LF;
+    int stride_log2;
+    DevStatus* st;
+};
+
+__global__ void __launch_bounds__(kThreads) k_inv_up(InvArgs a, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    int2 tl = a.tiles[blockIdx.x];
+    int b = tl.x, s0 = tl.y;
+    int bs = a.off[b], n = a.off[b + 1] - bs;
+    int j = (s0 - bs) / kInitTile;
+    int m = (n + kInitTile - 1) / kInitTile;
+    int end = min(bs + n, s0 + kInitTile);
+    for (int base = s0; base < end; base += kThreads) {
+        int x = base + threadIdx.x;
+        unsigned c = x < end ? (unsigned)a.U[x] : 256u;
+        unsigned peers = __match_any_sync(0xffffffffu, c);
+        if (c < 256u && lane_id() == (unsigned)(__ffs(peers) - 1)) atomicAdd(&h[c], __popc(peers));
+    }
+    __syncthreads();
+    hist[(size_t)256 * a.tbase[b] + (size_t)threadIdx.x * m + j] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kThreads) k_inv_down(InvArgs a, const uint32_t* __restrict__ hist) {
+    __shared__ uint32_t wcnt[kWarps][256];
+    __shared__ uint32_t base_of[256];
+    const unsigned w = warp_id(), ln = lane_id();
+    const unsigned lt_mask = (1u << ln) - 1u;
+    int2 tl = a.tiles[blockIdx.x];
+    int b = tl.x, s0 = tl.y;
+    int bs = a.off[b], n = a.off[b + 1] - bs;
+    int j = (s0 - bs) / kInitTile;
+    int m = (n + kInitTile - 1) / kInitTile;
+    int cnt = min(kInitTile, bs + n - s0);
+    int p = a.idx[b];
+    int* LF = a.LF + bs + b;  // rows of this block
+#pragma unroll
+    for (int q = 0; q < kWarps; ++q) wcnt[q][threadIdx.x] = 0;
+    __syncthreads();
+    uint8_t cc[kIRItems];
+    uint32_t rk[kIRItems];
+#pragma unroll
+    for (int it = 0; it < kIRItems; ++it) {
+        int i = (int)w * kIRWarpSpan + it * 32 + (int)ln;
+        bool valid = i < cnt;
+        unsigned c = valid ? (unsigned)a.U[s0 + i] : 256u;
+        unsigned peers = __match_any_sync(0xffffffffu, c);
+        unsigned before = __popc(peers & lt_mask);
+        uint32_t prev = valid ? wcnt[w][c] : 0u;
+        __syncwarp();
+        if (valid && before == 0) wcnt[w][c] = prev + __popc(peers);
+        __syncwarp();
+        cc[it] = (uint8_t)c;
+        rk[it] = prev + before;
+    }
+    __syncthreads();
+    {
+        unsigned c = threadIdx.x;
+        uint32_t run = 0;
+#pragma unroll
+        for (int q = 0; q < kWarps; ++q) {
+            uint32_t v = wcnt[q][c];
+            wcnt[q][c] = run;
+            run += v;
+        }
+        // rows before this tile's first c within the block, plus the sentinel row 0
+        base_of[c] = hist[(size_t)256 * a.tbase[b] + (size_t)c * m + j] - (uint32_t)bs + 1u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < kIRItems; ++it) {
+        int i = (int)w * kIRWarpSpan + it * 32 + (int)ln;
+        if (i < cnt) {
+            unsigned c = cc[it];
+            int u = s0 - bs + i;
+            int row = u < p ? u : u + 1;
+            LF[row] = (int)(base_of[c] + wcnt[w][c] + rk[it]);
+        }
+    }
+    if (j == 0 && threadIdx.x == 0) LF[p] = 0;
+}
+
+struct RulerArgs {
+    const int2* rtiles;  // (block, first local ruler) per CTA
+    int* next0;
+    int* dist0;
+    int* len;
+};
+
+__global__ void __launch_bounds__(kThreads) k_inv_walk1(InvArgs a, RulerArgs r) {
+    int2 rt = r.rtiles[blockIdx.x];
+    int b = rt.x;
+    int bs = a.off[b], n = a.off[b + 1] - bs;
+    int mask = (1 << a.stride_log2) - 1;
+    int M = (n >> a.stride_log2) + 1;
+    int lq = rt.y + threadIdx.x;
+    if (lq >= M) return;
+    const int* LF = a.LF + bs + b;
+    int q = a.rbase[b] + lq;
+    int cur = lq << a.stride_log2;
+    int steps = 0;
+    bool ok = true;
+    do {
+        cur = LF[cur];
+        ++steps;
+        if (cur < 0 || cur > n || steps > n + 1) {
+            ok = false;
+            break;
+        }
+    } while (cur & mask);
+    if (!ok) {
+        report(a.st, QZGPU_DATA_CORRUPT, 10, b);
+        r.next0[q] = -1;
+        r.dist0[q] = 0;
+        r.len[q] = 0;
+        return;
+    }
+    int nl = cur >> a.stride_log2;
+    r.next0[q] = nl == 0 ? -1 : a.rbase[b] + nl;
+    r.dist0[q] = steps;
+    r.len[q] = steps;
+}
+
+// One pointer-jumping step over all rulers: dist += dist[next], next = next[next].
+__global__ void __launch_bounds__(kThreads) k_inv_jump(int M, const int* __restrict__ nin,
+                                                       const int* __restrict__ din, int* __restrict__ nout,
+                                                       int* __restrict__ dout) {
+    for (int q = blockIdx.x * kThreads + threadIdx.x; q < M; q += gridDim.x * kThreads) {
+        int nx = nin[q];
+        int d = din[q];
+        if (nx >= 0) {
+            d += din[nx];
+            nx = nin[nx];
+        }
+        nout[q] = nx;
+        dout[q] = d;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_inv_walk2(InvArgs a, RulerArgs r, const int* __restrict__ next,
+                                                        const int* __restrict__ dist,
+                                                        const uint32_t* __restrict__ hist,
+                                                        uint8_t* __restrict__ T) {
+    __shared__ int C[257];
+    int2 rt = r.rtiles[blockIdx.x];
+    int b = rt.x;
+    int bs = a.off[b], n = a.off[b + 1] - bs;
+    int m = (n + kInitTile - 1) / kInitTile;
+    // symbol starts in the first column: 1 + count of smaller symbols
+    C[threadIdx.x] = (int)(hist[(size_t)256 * a.tbase[b] + (size_t)threadIdx.x * m] - (uint32_t)bs) + 1;
+    if (threadIdx.x == 0) C[256] = n + 1;
+    __syncthreads();
+    int M = (n >> a.stride_log2) + 1;
+    int lq = rt.y + threadIdx.x;
+    if (lq >= M) return;
+    const int* LF = a.LF + bs + b;
+    int q = a.rbase[b] + lq;
+    if (lq == 0 && (next[q] != -1 || dist[q] != n + 1)) {
+        report(a.st, QZGPU_DATA_CORRUPT, 11, b);
+        return;
+    }
+    int d = (n + 1) - dist[q];
+    int cur = lq << a.stride_log2;
+    int L = r.len[q];
+    if (d < 0 || d > n) {
+        report(a.st, QZGPU_DATA_CORRUPT, 12, b);
+        return;
+    }
+    for (int t = 0; t < L; ++t) {
+        int s = n - d;
+        if (s < 0) {
+            report(a.st, QZGPU_DATA_CORRUPT, 13, b);
+            return;
+        }
+        if (s < n) {
+            int lo = 0, hi = 255;
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (C[mid] <= cur) lo = mid; else hi = mid - 1;
+            }
+            T[bs + s] = (uint8_t)lo;
+        }
+        cur = LF[cur];
+        ++d;
+    }
+}
+
+int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t* d_U, uint8_t* d_T,
+                cudaStream_t st) {
+    if (nb < 0 || nb > S->cap_blocks) return QZGPU_BAD_PARAMETER;
+    long long N = 0;
+    for (int b = 0; b < nb; ++b) {
+        if (n[b] < 0) return QZGPU_BAD_PARAMETER;
+        if (n[b] > 0 && (idx[b] < 1 || idx[b] > n[b])) return QZGPU_DATA_CORRUPT;
+        N += n[b];
+    }
+    if (N > S->cap_bytes) return QZGPU_BAD_PARAMETER;
+    S->stats = qzgpu_stats{};
+    if (N == 0) return QZGPU_NO_ERROR;
+    int launches = 0;
+    const int stride_log2 = 5;  // rulers every 32 rows
+    const int stride = 1 << stride_log2;
+
+    std::vector<int> off(nb + 1, 0), tbase(nb + 1, 0), rbase(nb + 1, 0);
+    std::vector<int2> tiles, rtiles;
+    int maxM = 1;
+    for (int b = 0; b < nb; ++b) {
+        off[b + 1] = off[b] + n[b];
+        int m = (n[b] + kInitTile - 1) / kInitTile;
+        tbase[b + 1] = tbase[b] + m;
+        for (int s = off[b]; s < off[b + 1]; s += kInitTile) tiles.push_back(make_int2(b, s));
+        int M = n[b] > 0 ? n[b] / stride + 1 : 0;
+        rbase[b + 1] = rbase[b] + M;
+        for (int q = 0; q < M; q += kThreads) rtiles.push_back(make_int2(b, q));
+        if (M > maxM) maxM = M;
+    }
+    int Mtot = rbase[nb];
+    if ((size_t)tbase[nb] * 256 > S->hist_cap) return QZGPU_BAD_PARAMETER;
+    size_t need = sizeof(int) * (4 * (nb + 1)) + sizeof(int2) * (tiles.size() + rtiles.size()) + 256;
+    if (need > S->pin_tab_bytes) return QZGPU_BAD_PARAMETER;
+    char* p = S->pin_tab;
+    auto put = [&](const void* src, size_t bytes) {
+        char* at = p;
+        if (bytes) memcpy(p, src, bytes);
+        p += (bytes + 15) / 16 * 16;
+        return at;
+    };
+    char* h_off = put(off.data(), sizeof(int) * off.size());
+    char* h_idx = put(idx, sizeof(int) * nb);
+    char* h_tb = put(tbase.data(), sizeof(int) * tbase.size());
+    char* h_rb = put(rbase.data(), sizeof(int) * rbase.size());
+    char* h_tiles = put(tiles.data(), sizeof(int2) * tiles.size());
+    char* h_rt = put(rtiles.data(), sizeof(int2) * rtiles.size());
+    cudaError_t e = cudaSuccess;
+    auto h2d = [&](void* dst, const char* src, size_t bytes) {
+        if (bytes && e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+    };
+    InvBuffers& v = S->v;
+    h2d(S->blk_off, h_off, sizeof(int) * off.size());
+    h2d(S->blk_idx, h_idx, sizeof(int) * nb);
+    h2d(S->blk_tbase, h_tb, sizeof(int) * tbase.size());
+    h2d(S->blk_aux_off, h_rb, sizeof(int) * rbase.size());  // ruler bases reuse this table
+    h2d(S->tiles, h_tiles, sizeof(int2) * tiles.size());
+    h2d(v.rtiles, h_rt, sizeof(int2) * rtiles.size());
+    if (e == cudaSuccess) e = cudaMemsetAsync(S->status, 0, sizeof(DevStatus), st);
+    if (e != cudaSuccess) return map_cuda_error(e);
+
+    InvArgs a{d_U, S->blk_off, S->blk_idx, S->blk_tbase, S->blk_aux_off, S->tiles, v.LF, stride_log2, S->status};
+    int ntiles = (int)tiles.size();
+    int hist_len = tbase[nb] * 256;
+    k_inv_up<<<ntiles, kThreads, 0, st>>>(a, S->hist);
+    scan_exclusive(S->hist, S->hist, hist_len, nullptr, S->partial, nullptr, st, &launches);
+    k_inv_down<<<ntiles, kThreads, 0, st>>>(a, S->hist);
+    launches += 2;
+    RulerArgs r{v.rtiles, v.rnext[0], v.rdist[0], v.rlen};
+    int nrt = (int)rtiles.size();
+    k_inv_walk1<<<nrt, kThreads, 0, st>>>(a, r);
+    ++launches;
+    int it = 0;
+    int cur = 0;
+    int jgrid = (int)std::min<long long>(((long long)Mtot + kThreads - 1) / kThreads, (long long)S->sms * 16);
+    for (long long span = 1; span < maxM + 1; span <<= 1) {
+        k_inv_jump<<<jgrid, kThreads, 0, st>>>(Mtot, v.rnext[cur], v.rdist[cur], v.rnext[cur ^ 1], v.rdist[cur ^ 1]);
+        ++launches;
+        cur ^= 1;
+        ++it;
+    }
+    k_inv_walk2<<<nrt, kThreads, 0, st>>>(a, r, v.rnext[cur], v.rdist[cur], S->hist, d_T);
+    ++launches;
+    DevStatus* hst = reinterpret_cast<DevStatus*>(S->pin_rd);
+    e = cudaMemcpyAsync(hst, S->status, sizeof(DevStatus), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return map_cuda_error(e);
+    if (hst->error) return hst->error;
+    S->stats.kernel_launches = launches;
+    S->stats.alg_bytes = 12 * N;
+    return QZGPU_NO_ERROR;
+}
+
+}  // namespace qz

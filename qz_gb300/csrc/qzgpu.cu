@@ -1,0 +1,507 @@
+// C ABI of the block-sorting library (declared in include/qzgpu.h): device
+// scratch storages, a pool of them for the single-block libbsc-style calls,
+// and host-buffer / device-buffer entry points.
+#include <algorithm>
+#include <condition_variable>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "engine.h"
+
+namespace qz {
+
+int map_cuda_error(cudaError_t e) {
+    switch (e) {
+        case cudaSuccess: return QZGPU_NO_ERROR;
+        case cudaErrorMemoryAllocation: return QZGPU_GPU_NOT_ENOUGH_MEMORY;
+        case cudaErrorNoDevice:
+        case cudaErrorInsufficientDriver:
+        case cudaErrorNoKernelImageForDevice: return QZGPU_GPU_NOT_SUPPORTED;
+        default: return QZGPU_GPU_ERROR;
+    }
+}
+
+namespace {
+
+constexpr size_t kAlign = 256;
+constexpr int kMinStrideLog2 = 3;  // the inverse never uses rulers denser than every 8 rows
+
+struct Carver {
+    char* base;
+    size_t off = 0;
+    template <typename T>
+    T* take(size_t count) {
+        off = (off + kAlign - 1) / kAlign * kAlign;
+        T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+        off += count * sizeof(T);
+        return p;
+    }
+};
+
+struct Caps {
+    size_t N, nb, init_tiles, hist, small, med, large, rulers, rtiles, aux;
+};
+
+Caps caps_for(long long cap_bytes, int cap_blocks) {
+    Caps c;
+    c.N = (size_t)cap_bytes;
+    c.nb = (size_t)cap_blocks;
+    c.init_tiles = c.N / kInitTile + c.nb + 1;
+    size_t fwd_tiles = 2 * (c.N / kRT) + 2;
+    c.hist = 256 * std::max(fwd_tiles, c.init_tiles);
+    c.small = c.N / 2 + 1;
+    c.med = c.N / (kSmallMax + 1) + 1;
+    c.large = c.N / (kMedMax + 1) + 2;
+    c.rulers = (c.N >> kMinStrideLog2) + c.nb + 1;
+    c.rtiles = c.rulers / kThreads + c.nb + 1;
+    c.aux = 64 * c.nb + 64;
+    return c;
+}
+
+// Lays the device buffers out from `base` (null: only measure).
+size_t layout(Storage* S, char* base, const Caps& c) {
+    Carver cv{base};
+    Storage tmp;
+    Storage* s = S ? S : &tmp;
+    s->T = cv.take<uint8_t>(c.N + 64);
+    s->U = cv.take<uint8_t>(c.N + 64);
+    s->hist = cv.take<uint32_t>(c.hist);
+    s->hist_cap = c.hist;
+    s->partial = cv.take<uint32_t>(1024);
+    s->split_part = cv.take<int>(2 * kSplitGrid);
+    s->counters = cv.take<int>(64);
+    s->status = cv.take<DevStatus>(1);
+    s->blk_off = cv.take<int>(c.nb + 1);
+    s->blk_K = cv.take<int>(c.nb + 1);
+    s->blk_sigma = cv.take<int>(c.nb + 1);
+    s->blk_code = cv.take<uint8_t>(256 * c.nb);
+    s->blk_hist = cv.take<uint32_t>(256 * c.nb);
+    s->blk_idx = cv.take<int>(c.nb + 1);
+    s->blk_aux_rate = cv.take<int>(c.nb + 1);
+    s->blk_aux_off = cv.take<int>(c.nb + 1);
+    s->blk_tbase = cv.take<int>(c.nb + 1);
+    s->aux = cv.take<int>(c.aux);
+    s->tiles = cv.take<int2>(c.init_tiles);
+    size_t shared_start = cv.off;
+    // forward layout
+    FwdBuffers& f = s->f;
+    f.SA = cv.take<int>(c.N);
+    f.R = cv.take<int>(c.N);
+    f.key = cv.take<uint32_t>(c.N);
+    for (int i = 0; i < 2; ++i) {
+        f.W[i] = cv.take<int>(c.N);
+        f.P[i] = cv.take<int>(c.N);
+        f.G[i] = cv.take<int>(c.N);
+        f.wsk[i] = cv.take<uint32_t>(c.N);
+        f.wsv[i] = cv.take<int>(c.N);
+    }
+    f.list[0] = cv.take<int2>(c.small);
+    f.list[1] = cv.take<int2>(c.med);
+    f.list[2] = cv.take<int2>(c.large);
+    f.ltc = cv.take<uint32_t>(c.large + 1);
+    f.llen = cv.take<uint32_t>(c.large + 1);
+    f.ltbase = cv.take<uint32_t>(c.large + 1);
+    f.lwbase = cv.take<uint32_t>(c.large + 1);
+    size_t fwd_end = cv.off;
+    // inverse layout, aliasing the forward buffers
+    cv.off = shared_start;
+    InvBuffers& v = s->v;
+    v.LF = cv.take<int>(c.N + c.nb + 1);
+    for (int i = 0; i < 2; ++i) {
+        v.rnext[i] = cv.take<int>(c.rulers);
+        v.rdist[i] = cv.take<int>(c.rulers);
+    }
+    v.rlen = cv.take<int>(c.rulers);
+    v.rrow = nullptr;
+    v.rtiles = cv.take<int2>(c.rtiles);
+    return std::max(fwd_end, cv.off) + kAlign;
+}
+
+size_t pinned_table_bytes(const Caps& c) {
+    return sizeof(int) * 8 * (c.nb + 1) + sizeof(int2) * (c.init_tiles + c.rtiles + 3 * c.nb + 8) +
+           sizeof(int) * 64 + 4096;
+}
+
+// ---------------------------------------------------------------- global state
+
+struct Global {
+    std::mutex mu;
+    bool inited = false;
+    int device = 0;
+    int sms = 0;
+    // pool of storages for the single-block drop-in calls
+    std::condition_variable cv;
+    std::vector<std::unique_ptr<Storage>> pool;
+    std::vector<Storage*> idle;
+    int pool_max = 4;
+    long long pool_cap = 32ll << 20;  // covers qz's 25 MiB blocks
+};
+
+Global& G() {
+    static Global g;
+    return g;
+}
+
+int ensure_init() {
+    Global& g = G();
+    std::lock_guard<std::mutex> lk(g.mu);
+    if (g.inited) return QZGPU_NO_ERROR;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return map_cuda_error(e);
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return map_cuda_error(e);
+    g.device = dev;
+    g.sms = sms;
+    g.inited = true;
+    const char* env = getenv("QZGPU_POOL_STORAGES");
+    if (env && atoi(env) > 0) g.pool_max = atoi(env);
+    return QZGPU_NO_ERROR;
+}
+
+Storage* pool_acquire(long long need) {
+    Global& g = G();
+    std::unique_lock<std::mutex> lk(g.mu);
+    for (;;) {
+        for (size_t i = 0; i < g.idle.size(); ++i) {
+            if (g.idle[i]->cap_bytes >= need) {
+                Storage* s = g.idle[i];
+                g.idle.erase(g.idle.begin() + (long)i);
+                return s;
+            }
+        }
+        if ((int)g.pool.size() < g.pool_max) {
+            auto s = std::make_unique<Storage>();
+            lk.unlock();
+            int rc = storage_init(s.get(), std::max(need, g.pool_cap), 1);
+            lk.lock();
+            if (rc != QZGPU_NO_ERROR) return nullptr;
+            g.pool.push_back(std::move(s));
+            return g.pool.back().get();
+        }
+        g.cv.wait(lk);
+    }
+}
+
+void pool_release(Storage* s) {
+    Global& g = G();
+    {
+        std::lock_guard<std::mutex> lk(g.mu);
+        g.idle.push_back(s);
+    }
+    g.cv.notify_one();
+}
+
+}  // namespace
+
+size_t storage_device_bytes(long long cap_bytes, int cap_blocks) {
+    return layout(nullptr, nullptr, caps_for(cap_bytes, cap_blocks));
+}
+
+int storage_init(Storage* S, long long cap_bytes, int cap_blocks) {
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (cap_bytes < 1 || cap_blocks < 1 || cap_bytes > QZGPU_MAX_BATCH_BYTES) return QZGPU_BAD_PARAMETER;
+    Global& g = G();
+    cudaError_t e = cudaSetDevice(g.device);
+    if (e != cudaSuccess) return map_cuda_error(e);
+    Caps c = caps_for(cap_bytes, cap_blocks);
+    S->cap_bytes = cap_bytes;
+    S->cap_blocks = cap_blocks;
+    S->device = g.device;
+    S->sms = g.sms;
+    size_t bytes = layout(nullptr, nullptr, c);
+    e = cudaMalloc(&S->dev, bytes);
+    if (e != cudaSuccess) {
+        S->dev = nullptr;
+        return map_cuda_error(e);
+    }
+    S->dev_bytes = bytes;
+    layout(S, S->dev, c);
+    S->pin_tab_bytes = pinned_table_bytes(c);
+    size_t rd = sizeof(int) * (c.nb + 256);
+    S->pin_bytes = 2 * (c.N + 64) + S->pin_tab_bytes + rd + 64;
+    e = cudaMallocHost(&S->pin, S->pin_bytes);
+    if (e != cudaSuccess) {
+        cudaFree(S->dev);
+        S->dev = nullptr;
+        S->pin = nullptr;
+        return QZGPU_NOT_ENOUGH_MEMORY;
+    }
+    S->pin_T = reinterpret_cast<uint8_t*>(S->pin);
+    S->pin_U = S->pin_T + c.N + 64;
+    S->pin_tab = reinterpret_cast<char*>(S->pin_U + c.N + 64);
+    S->pin_rd = reinterpret_cast<int*>(S->pin_tab + S->pin_tab_bytes);
+    e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        storage_free(S);
+        return map_cuda_error(e);
+    }
+    return QZGPU_NO_ERROR;
+}
+
+void storage_free(Storage* S) {
+    if (S->stream) cudaStreamDestroy(S->stream);
+    if (S->dev) cudaFree(S->dev);
+    if (S->pin) cudaFreeHost(S->pin);
+    S->stream = nullptr;
+    S->dev = nullptr;
+    S->pin = nullptr;
+}
+
+}  // namespace qz
+
+using namespace qz;
+
+struct qzgpu_storage : public qz::Storage {};
+
+namespace {
+
+int check_blocks(int nblocks, const int* n, long long* total) {
+    if (nblocks < 0 || (nblocks > 0 && !n)) return QZGPU_BAD_PARAMETER;
+    long long t = 0;
+    for (int b = 0; b < nblocks; ++b) {
+        if (n[b] < 0 || n[b] > QZGPU_MAX_BLOCK) return QZGPU_BAD_PARAMETER;
+        t += n[b];
+    }
+    *total = t;
+    return QZGPU_NO_ERROR;
+}
+
+// Host-buffer forward batch on storage S (caller holds S->mu).
+int encode_host(Storage* S, int nb, const unsigned char* const* T, unsigned char* const* U, const int* n,
+                int* idx, const int* aux_rate, int* aux_out) {
+    cudaError_t e = cudaSetDevice(S->device);
+    if (e != cudaSuccess) return map_cuda_error(e);
+    long long off = 0;
+    for (int b = 0; b < nb; ++b) {
+        if (n[b] > 0) {
+            e = cudaMemcpyAsync(S->T + off, T[b], (size_t)n[b], cudaMemcpyHostToDevice, S->stream);
+            if (e != cudaSuccess) return map_cuda_error(e);
+        }
+        off += n[b];
+    }
+    int rc = forward_run(S, nb, n, S->T, S->U, idx, aux_rate, aux_out, S->stream);
+    if (rc) return rc;
+    off = 0;
+    for (int b = 0; b < nb; ++b) {
+        if (n[b] > 0) {
+            e = cudaMemcpyAsync(U[b], S->U + off, (size_t)n[b], cudaMemcpyDeviceToHost, S->stream);
+            if (e != cudaSuccess) return map_cuda_error(e);
+        }
+        off += n[b];
+    }
+    e = cudaStreamSynchronize(S->stream);
+    return map_cuda_error(e);
+}
+
+int decode_host(Storage* S, int nb, const unsigned char* const* U, unsigned char* const* T, const int* n,
+                const int* idx) {
+    cudaError_t e = cudaSetDevice(S->device);
+    if (e != cudaSuccess) return map_cuda_error(e);
+    long long off = 0;
+    for (int b = 0; b < nb; ++b) {
+        if (n[b] > 0) {
+            e = cudaMemcpyAsync(S->U + off, U[b], (size_t)n[b], cudaMemcpyHostToDevice, S->stream);
+            if (e != cudaSuccess) return map_cuda_error(e);
+        }
+        off += n[b];
+    }
+    int rc = inverse_run(S, nb, n, idx, S->U, S->T, S->stream);
+    if (rc) return rc;
+    off = 0;
+    for (int b = 0; b < nb; ++b) {
+        if (n[b] > 0) {
+            e = cudaMemcpyAsync(T[b], S->T + off, (size_t)n[b], cudaMemcpyDeviceToHost, S->stream);
+            if (e != cudaSuccess) return map_cuda_error(e);
+        }
+        off += n[b];
+    }
+    e = cudaStreamSynchronize(S->stream);
+    return map_cuda_error(e);
+}
+
+// Runs fn on a pooled storage that fits `need` bytes (or a temporary one).
+template <typename Fn>
+int with_pooled(long long need, Fn fn) {
+    int rc = ensure_init();
+    if (rc) return rc;
+    if (need > G().pool_cap) {
+        Storage tmp;
+        rc = storage_init(&tmp, need, 1);
+        if (rc) return rc;
+        rc = fn(&tmp);
+        storage_free(&tmp);
+        return rc;
+    }
+    Storage* s = pool_acquire(need);
+    if (!s) return QZGPU_GPU_NOT_ENOUGH_MEMORY;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        rc = fn(s);
+    }
+    pool_release(s);
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qzgpu_init(int features) {
+    (void)features;
+    return ensure_init();
+}
+
+const char* qzgpu_error_string(int code) {
+    switch (code) {
+        case QZGPU_NO_ERROR: return "no error";
+        case QZGPU_BAD_PARAMETER: return "bad parameter";
+        case QZGPU_NOT_ENOUGH_MEMORY: return "not enough host memory";
+        case QZGPU_NOT_COMPRESSIBLE: return "not compressible";
+        case QZGPU_NOT_SUPPORTED: return "not supported";
+        case QZGPU_UNEXPECTED_EOB: return "unexpected end of block";
+        case QZGPU_DATA_CORRUPT: return "data corrupt";
+        case QZGPU_GPU_ERROR: return "GPU error";
+        case QZGPU_GPU_NOT_SUPPORTED: return "no usable GPU";
+        case QZGPU_GPU_NOT_ENOUGH_MEMORY: return "not enough GPU memory";
+        case QZGPU_TIMEOUT: return "timed out";
+        default: return "unknown error";
+    }
+}
+
+int qzgpu_aux_rate(int n) {
+    int x = n / 8;
+    if (x < 1) return 1;
+    int r = 1;
+    while ((r << 1) <= x) r <<= 1;
+    return r;
+}
+
+int qzgpu_bwt_encode(unsigned char* T, int n, unsigned char* num_indexes, int* indexes, int features) {
+    (void)features;
+    if (n < 0 || (n > 0 && !T)) return QZGPU_BAD_PARAMETER;
+    if (num_indexes) *num_indexes = 0;
+    if (n <= 1) return n;
+    int rate = qzgpu_aux_rate(n);
+    int naux = (n - 1) / rate;
+    bool want_aux = indexes && num_indexes && naux <= 255;
+    int idx = 0;
+    int rc = with_pooled(n, [&](Storage* s) {
+        const unsigned char* in[1] = {T};
+        unsigned char* out[1] = {T};
+        return encode_host(s, 1, in, out, &n, &idx, want_aux ? &rate : nullptr, want_aux ? indexes : nullptr);
+    });
+    if (rc) return rc;
+    if (want_aux) *num_indexes = (unsigned char)naux;
+    return idx;
+}
+
+int qzgpu_bwt_decode(unsigned char* T, int n, int index, unsigned char num_indexes, const int* indexes,
+                     int features) {
+    (void)features;
+    (void)num_indexes;
+    (void)indexes;
+    if (n < 0 || (n > 0 && !T)) return QZGPU_BAD_PARAMETER;
+    if (n == 0) return QZGPU_NO_ERROR;
+    if (index < 1 || index > n) return QZGPU_DATA_CORRUPT;
+    if (n == 1) return QZGPU_NO_ERROR;
+    return with_pooled(n, [&](Storage* s) {
+        const unsigned char* in[1] = {T};
+        unsigned char* out[1] = {T};
+        return decode_host(s, 1, in, out, &n, &index);
+    });
+}
+
+long long qzgpu_storage_bytes(long long max_total_bytes, int max_blocks) {
+    if (max_total_bytes < 1 || max_blocks < 1) return 0;
+    return (long long)storage_device_bytes(max_total_bytes, max_blocks);
+}
+
+int qzgpu_storage_create(qzgpu_storage** storage, long long max_total_bytes, int max_blocks) {
+    if (!storage) return QZGPU_BAD_PARAMETER;
+    *storage = nullptr;
+    auto* s = new (std::nothrow) qzgpu_storage();
+    if (!s) return QZGPU_NOT_ENOUGH_MEMORY;
+    int rc = storage_init(s, max_total_bytes, max_blocks);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *storage = s;
+    return QZGPU_NO_ERROR;
+}
+
+int qzgpu_storage_destroy(qzgpu_storage* storage) {
+    if (!storage) return QZGPU_BAD_PARAMETER;
+    {
+        std::lock_guard<std::mutex> lk(storage->mu);
+        cudaSetDevice(storage->device);
+        storage_free(storage);
+    }
+    delete storage;
+    return QZGPU_NO_ERROR;
+}
+
+int qzgpu_bwt_encode_batch(qzgpu_storage* storage, int nblocks, const unsigned char* const* T,
+                           unsigned char* const* U, const int* n, int* indexes, int features) {
+    (void)features;
+    long long total;
+    int rc = check_blocks(nblocks, n, &total);
+    if (rc) return rc;
+    if (!storage || (nblocks > 0 && (!T || !U || !indexes))) return QZGPU_BAD_PARAMETER;
+    std::lock_guard<std::mutex> lk(storage->mu);
+    if (total > storage->cap_bytes || nblocks > storage->cap_blocks) return QZGPU_BAD_PARAMETER;
+    return encode_host(storage, nblocks, T, U, n, indexes, nullptr, nullptr);
+}
+
+int qzgpu_bwt_decode_batch(qzgpu_storage* storage, int nblocks, const unsigned char* const* U,
+                           unsigned char* const* T, const int* n, const int* indexes, int features) {
+    (void)features;
+    long long total;
+    int rc = check_blocks(nblocks, n, &total);
+    if (rc) return rc;
+    if (!storage || (nblocks > 0 && (!T || !U || !indexes))) return QZGPU_BAD_PARAMETER;
+    std::lock_guard<std::mutex> lk(storage->mu);
+    if (total > storage->cap_bytes || nblocks > storage->cap_blocks) return QZGPU_BAD_PARAMETER;
+    return decode_host(storage, nblocks, U, T, n, indexes);
+}
+
+int qzgpu_bwt_encode_device(qzgpu_storage* storage, int nblocks, const int* n, const unsigned char* d_T,
+                            unsigned char* d_U, int* indexes, void* stream) {
+    long long total;
+    int rc = check_blocks(nblocks, n, &total);
+    if (rc) return rc;
+    if (!storage || (total > 0 && (!d_T || !d_U || !indexes)) || d_T == d_U) return QZGPU_BAD_PARAMETER;
+    std::lock_guard<std::mutex> lk(storage->mu);
+    if (total > storage->cap_bytes || nblocks > storage->cap_blocks) return QZGPU_BAD_PARAMETER;
+    cudaError_t e = cudaSetDevice(storage->device);
+    if (e != cudaSuccess) return map_cuda_error(e);
+    return forward_run(storage, nblocks, n, d_T, d_U, indexes, nullptr, nullptr,
+                       reinterpret_cast<cudaStream_t>(stream));
+}
+
+int qzgpu_bwt_decode_device(qzgpu_storage* storage, int nblocks, const int* n, const int* indexes,
+                            const unsigned char* d_U, unsigned char* d_T, void* stream) {
+    long long total;
+    int rc = check_blocks(nblocks, n, &total);
+    if (rc) return rc;
+    if (!storage || (total > 0 && (!d_T || !d_U || !indexes)) || d_T == d_U) return QZGPU_BAD_PARAMETER;
+    std::lock_guard<std::mutex> lk(storage->mu);
+    if (total > storage->cap_bytes || nblocks > storage->cap_blocks) return QZGPU_BAD_PARAMETER;
+    cudaError_t e = cudaSetDevice(storage->device);
+    if (e != cudaSuccess) return map_cuda_error(e);
+    return inverse_run(storage, nblocks, n, indexes, d_U, d_T, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int qzgpu_storage_last_stats(const qzgpu_storage* storage, qzgpu_stats* out) {
+    if (!storage || !out) return QZGPU_BAD_PARAMETER;
+    *out = storage->stats;
+    return QZGPU_NO_ERROR;
+}
+
+}  // extern "C"

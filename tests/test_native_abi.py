@@ -1,0 +1,73 @@
+"""The C-ABI library builds, loads and exports every entry point the header
+declares (no compute calls: this runs without a GPU)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from qz_gb300 import build, native
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "qzgpu.h")
+
+
+def declared_functions(path=HEADER):
+    src = open(path).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(qzgpu_[a-z0-9_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return native.load()
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for must in ("qzgpu_init", "qzgpu_bwt_encode", "qzgpu_bwt_decode", "qzgpu_bwt_encode_batch",
+                 "qzgpu_bwt_decode_batch", "qzgpu_bwt_encode_device", "qzgpu_bwt_decode_device"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", native.LIB_PATH], capture_output=True, text=True,
+                         check=True).stdout
+    exported = set(re.findall(r"\sT\s+(\w+)", out))
+    missing = [f for f in declared_functions() if f not in exported]
+    assert not missing, missing
+    for f in declared_functions():
+        assert f in native.SIGNATURES, f"binding lacks {f}"
+        getattr(lib, f)
+
+
+def test_error_strings_and_aux_rate(lib):
+    assert native.error_string(-6) == "data corrupt"
+    assert native.error_string(0) == "no error"
+    # largest power of two <= max(n/8, 1)
+    assert lib.qzgpu_aux_rate(0) == 1
+    assert lib.qzgpu_aux_rate(7) == 1
+    assert lib.qzgpu_aux_rate(16) == 2
+    assert lib.qzgpu_aux_rate(26_214_400) == 2_097_152
+
+
+def test_kernels_built_for_sm103a(lib):
+    # one -gencode target, sm_103a, for every translation unit
+    assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+    objs = [os.path.join(build.OUT, os.path.basename(s) + ".o") for s in build.sources()]
+    assert all(os.path.exists(o) for o in objs)
+
+
+def test_no_cpu_fallback_without_gpu(lib):
+    # With no usable GPU the library reports an error instead of computing.
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from qz_gb300 import bwt
+
+    with pytest.raises(native.QzGpuError) as e:
+        bwt.bwt_encode(b"ACGTACGT")
+    assert e.value.code in (native.QZGPU_GPU_NOT_SUPPORTED, native.QZGPU_GPU_ERROR)
