@@ -22,12 +22,14 @@ constexpr int kMaxRounds = 40;   // prefix doubling needs <= 31 rounds for n < 2
 
 // Device counters (int32 slots of Storage::counters).
 enum Counter {
-    CNT_ACTIVE = 0,  // suffixes still in non-singleton groups
+    CNT_ACTIVE = 0,  // suffixes still in non-singleton groups (two slots: 0 and 6,
+                     // a split reads one and writes the other)
     CNT_SMALL = 1,   // descriptor counts per class
     CNT_MED = 2,
     CNT_LARGE = 3,
     CNT_LTILES = 4,  // tiles of the large-group radix sort
     CNT_LHIST = 5,   // histogram entries of the large-group radix sort (256 per tile)
+    CNT_ACTIVE_ALT = 6,
     CNT_SLOTS = 16,
 };
 
@@ -122,5 +124,19 @@ int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t*
                 cudaStream_t st);
 
 int map_cuda_error(cudaError_t e);
+
+// Debug mode (environment QZGPU_DEBUG=1): every launch is followed by a
+// stream synchronize and an error check, and failures are logged to stderr.
+bool debug_on();
+void debug_after(cudaStream_t st, const char* what);
+void debug_log(const char* fmt, ...);
+// Dump mode (environment QZGPU_DUMP=<dir>): writes device arrays of small
+// batches to <dir>/<seq>_<name>.bin for offline inspection.
+bool dump_on();
+void dump_array(const char* name, const void* dptr, size_t bytes, cudaStream_t st);
+#define QZ_DBG(st, what)                              \
+    do {                                              \
+        if (::qz::debug_on()) ::qz::debug_after(st, what); \
+    } while (0)
 
 }  // namespace qz

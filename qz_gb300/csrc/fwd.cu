@@ -358,7 +358,8 @@ __global__ void __launch_bounds__(kThreads) k_large_down(LargeArgs a, const uint
 // ------------------------------------------------------------------ split into groups
 
 struct SplitArgs {
-    const int* A;
+    const int* A;      // active slots of this split
+    int* A_next;       // receives the survivor count
     const uint32_t* key;
     const int* G;
     const int* P;  // null: slot k is SA position k (first split)
@@ -491,7 +492,7 @@ __global__ void __launch_bounds__(kThreads) k_split_top(SplitArgs a) {
         mcarry = max(mcarry, mtot);
     }
     if (threadIdx.x == 0) {
-        a.counters[CNT_ACTIVE] = (int)carry;
+        *a.A_next = (int)carry;
         a.counters[CNT_SMALL] = 0;
         a.counters[CNT_MED] = 0;
         a.counters[CNT_LARGE] = 0;
@@ -681,15 +682,18 @@ void sort_groups(Storage* S, const int* host_counts, uint32_t* key, int* W, cons
     int nsm = host_counts[CNT_SMALL], nmd = host_counts[CNT_MED], nlg = host_counts[CNT_LARGE];
     if (nsm > 0) {
         k_sort_small<<<grid_for(nsm, kThreads, L.sms * 16), kThreads, 0, L.st>>>(f.list[0], cnt + CNT_SMALL, key, W);
+        QZ_DBG(L.st, "k_sort_small");
         ++*L.launches;
     }
     if (nmd > 0) {
         k_sort_medium<<<grid_for(nmd, 1, L.sms * 4), kThreads, 0, L.st>>>(f.list[1], cnt + CNT_MED, key, W);
+        QZ_DBG(L.st, "k_sort_medium");
         ++*L.launches;
     }
     if (nlg > 0) {
         k_large_prep<<<grid_for(nlg, kThreads, L.sms * 4), kThreads, 0, L.st>>>(f.list[2], cnt + CNT_LARGE, f.ltc,
                                                                                  f.llen);
+        QZ_DBG(L.st, "k_large_prep");
         ++*L.launches;
         scan_exclusive(f.ltc, f.ltbase, 0, cnt + CNT_LARGE, S->partial, (uint32_t*)(cnt + CNT_LTILES), L.st,
                        L.launches);
@@ -704,11 +708,13 @@ void sort_groups(Storage* S, const int* host_counts, uint32_t* key, int* W, cons
         for (int pass = 0; pass < 4; ++pass) {
             int shift = 8 * pass;
             k_large_up<<<grid, kThreads, 0, L.st>>>(la, sk[pass], pass == 0, shift, S->hist);
+            QZ_DBG(L.st, "k_large_up");
             ++*L.launches;
             // histogram entries = 256 * tiles (count on device)
             scan_exclusive(S->hist, S->hist, 0, cnt + CNT_LHIST, S->partial, nullptr, L.st, L.launches);
             k_large_down<<<grid, kThreads, 0, L.st>>>(la, S->hist, sk[pass], sv[pass], pass == 0, dk[pass],
                                                       dv[pass], pass == 3, shift);
+            QZ_DBG(L.st, "k_large_down");
             ++*L.launches;
         }
     }
@@ -804,19 +810,36 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
     // ---- alphabet, initial keys
     int ntiles = (int)tiles.size();
     k_block_hist<<<ntiles, kThreads, 0, st>>>(d_T, S->tiles, S->blk_off, S->blk_hist);
+    QZ_DBG(st, "k_block_hist");
     k_block_alpha<<<nb, kThreads, 0, st>>>(S->blk_hist, S->blk_code, S->blk_K, S->blk_sigma);
+    QZ_DBG(st, "k_block_alpha");
     k_init_keys<<<ntiles, kThreads, 0, st>>>(d_T, S->tiles, S->blk_off, S->blk_code, S->blk_K, S->blk_sigma, f.key,
                                              f.W[0], f.G[0]);
+    QZ_DBG(st, "k_init_keys");
     launches += 3;
 
+    const bool dump = dump_on() && N <= (1 << 20);
+    if (dump) {
+        dump_array("init_key", f.key, 4 * N, st);
+        dump_array("init_W", f.W[0], 4 * N, st);
+        dump_array("init_G", f.G[0], 4 * N, st);
+        dump_array("blk_K", S->blk_K, 4 * nb, st);
+        dump_array("blk_sigma", S->blk_sigma, 4 * nb, st);
+    }
     // ---- initial sort (groups = blocks) and split
     int hc[CNT_SLOTS];
     memcpy(hc, cnt0, sizeof(hc));
     sort_groups(S, hc, f.key, f.W[0], L);
+    if (dump) {
+        dump_array("sorted_key", f.key, 4 * N, st);
+        dump_array("sorted_W", f.W[0], 4 * N, st);
+    }
     int cur = 0;
+    int act = CNT_ACTIVE;  // counter slot holding the current active count
     auto split = [&](const int* P) {
         SplitArgs a;
-        a.A = S->counters + CNT_ACTIVE;
+        a.A = S->counters + act;
+        a.A_next = S->counters + (act ^ (CNT_ACTIVE ^ CNT_ACTIVE_ALT));
         a.key = f.key;
         a.G = f.G[cur];
         a.P = P;
@@ -833,12 +856,29 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
         a.part_surv = S->split_part;
         a.part_head = S->split_part + kSplitGrid;
         k_split_count<<<kSplitGrid, kThreads, 0, st>>>(a);
+        QZ_DBG(st, "k_split_count");
         k_split_top<<<1, kThreads, 0, st>>>(a);
+        QZ_DBG(st, "k_split_top");
         k_split_apply<<<kSplitGrid, kThreads, 0, st>>>(a);
+        QZ_DBG(st, "k_split_apply");
         launches += 3;
         cur ^= 1;
+        act ^= CNT_ACTIVE ^ CNT_ACTIVE_ALT;
     };
     split(nullptr);
+    auto dump_split = [&]() {
+        if (!dump) return;
+        dump_array("split_counters", S->counters, 4 * CNT_SLOTS, st);
+        dump_array("split_R", f.R, 4 * N, st);
+        dump_array("split_SA", f.SA, 4 * N, st);
+        dump_array("split_P", f.P[cur], 4 * N, st);
+        dump_array("split_W", f.W[cur], 4 * N, st);
+        dump_array("split_G", f.G[cur], 4 * N, st);
+        dump_array("split_list0", f.list[0], 8 * N / 2, st);
+        dump_array("split_list1", f.list[1], 8 * (N / 17 + 1), st);
+        dump_array("split_part", S->split_part, 4 * 2 * kSplitGrid, st);
+    };
+    dump_split();
     S->rounds_active.push_back((int)N);
 
     int* hcnt = S->pin_rd;
@@ -847,15 +887,28 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
         e = cudaMemcpyAsync(hcnt, S->counters, sizeof(int) * CNT_SLOTS, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return map_cuda_error(e);
-        int A = hcnt[CNT_ACTIVE];
+        int A = hcnt[act];
         if (A == 0) break;
-        if (round >= kMaxRounds) return QZGPU_GPU_ERROR;
+        if (debug_on())
+            debug_log("round %d: active %d small %d medium %d large %d", round, A, hcnt[CNT_SMALL], hcnt[CNT_MED],
+                      hcnt[CNT_LARGE]);
+        if (round >= kMaxRounds) {
+            if (debug_on()) debug_log("no convergence after %d rounds", round);
+            return QZGPU_GPU_ERROR;
+        }
         S->rounds_active.push_back(A);
-        k_gather<<<grid_for(A, kThreads, S->sms * 16), kThreads, 0, st>>>(S->counters + CNT_ACTIVE, f.W[cur], f.R,
+        k_gather<<<grid_for(A, kThreads, S->sms * 16), kThreads, 0, st>>>(S->counters + act, f.W[cur], f.R,
                                                                           S->blk_off, nb, S->blk_K, round, f.key);
+        QZ_DBG(st, "k_gather");
         ++launches;
+        if (dump) dump_array("gather_key", f.key, 4 * (size_t)A, st);
         sort_groups(S, hcnt, f.key, f.W[cur], L);
+        if (dump) {
+            dump_array("rsorted_key", f.key, 4 * (size_t)A, st);
+            dump_array("rsorted_W", f.W[cur], 4 * (size_t)A, st);
+        }
         split(f.P[cur]);
+        dump_split();
         ++round;
     }
 
@@ -863,6 +916,7 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
     k_extract<<<grid_for(N, kThreads, S->sms * 16), kThreads, 0, st>>>(
         (int)N, f.SA, f.R, d_T, S->blk_off, nb, d_U, S->blk_idx, aux_rate ? S->blk_aux_rate : nullptr,
         S->blk_aux_off, S->aux, S->status);
+    QZ_DBG(st, "k_extract");
     ++launches;
     DevStatus& hst = *reinterpret_cast<DevStatus*>(S->pin_rd + S->cap_blocks + 64);
     e = cudaMemcpyAsync(hcnt, S->blk_idx, sizeof(int) * nb, cudaMemcpyDeviceToHost, st);
@@ -871,19 +925,25 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
         e = cudaMemcpyAsync(aux_out, S->aux, sizeof(int) * aux_total, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return map_cuda_error(e);
-    if (hst.error) return hst.error;
+    if (hst.error) {
+        if (debug_on()) debug_log("device status %d at %d detail %lld", hst.error, hst.where, hst.detail);
+        return hst.error;
+    }
     for (int b = 0; b < nb; ++b) {
         if (n[b] >= 2) {
-            if (hcnt[b] < 1 || hcnt[b] > n[b]) return QZGPU_GPU_ERROR;
+            if (hcnt[b] < 1 || hcnt[b] > n[b]) {
+                if (debug_on()) debug_log("block %d: primary index %d out of range (n %d)", b, hcnt[b], n[b]);
+                return QZGPU_GPU_ERROR;
+            }
             idx[b] = hcnt[b];
         }
     }
-    long long act = 0;
-    for (int a : S->rounds_active) act += a;
+    long long active_sum = 0;
+    for (int a : S->rounds_active) active_sum += a;
     S->stats.rounds = round;
     S->stats.kernel_launches = launches;
-    S->stats.active_total = act;
-    S->stats.alg_bytes = 15 * N + 28 * act;
+    S->stats.active_total = active_sum;
+    S->stats.alg_bytes = 15 * N + 28 * active_sum;
     return QZGPU_NO_ERROR;
 }
 

@@ -287,29 +287,37 @@ int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t*
     int ntiles = (int)tiles.size();
     int hist_len = tbase[nb] * 256;
     k_inv_up<<<ntiles, kThreads, 0, st>>>(a, S->hist);
+    QZ_DBG(st, "k_inv_up");
     scan_exclusive(S->hist, S->hist, hist_len, nullptr, S->partial, nullptr, st, &launches);
     k_inv_down<<<ntiles, kThreads, 0, st>>>(a, S->hist);
+    QZ_DBG(st, "k_inv_down");
     launches += 2;
     RulerArgs r{v.rtiles, v.rnext[0], v.rdist[0], v.rlen};
     int nrt = (int)rtiles.size();
     k_inv_walk1<<<nrt, kThreads, 0, st>>>(a, r);
+    QZ_DBG(st, "k_inv_walk1");
     ++launches;
     int it = 0;
     int cur = 0;
     int jgrid = (int)std::min<long long>(((long long)Mtot + kThreads - 1) / kThreads, (long long)S->sms * 16);
     for (long long span = 1; span < maxM + 1; span <<= 1) {
         k_inv_jump<<<jgrid, kThreads, 0, st>>>(Mtot, v.rnext[cur], v.rdist[cur], v.rnext[cur ^ 1], v.rdist[cur ^ 1]);
+        QZ_DBG(st, "k_inv_jump");
         ++launches;
         cur ^= 1;
         ++it;
     }
     k_inv_walk2<<<nrt, kThreads, 0, st>>>(a, r, v.rnext[cur], v.rdist[cur], S->hist, d_T);
+    QZ_DBG(st, "k_inv_walk2");
     ++launches;
     DevStatus* hst = reinterpret_cast<DevStatus*>(S->pin_rd);
     e = cudaMemcpyAsync(hst, S->status, sizeof(DevStatus), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return map_cuda_error(e);
-    if (hst->error) return hst->error;
+    if (hst->error) {
+        if (debug_on()) debug_log("device status %d at %d detail %lld", hst->error, hst->where, hst->detail);
+        return hst->error;
+    }
     S->stats.kernel_launches = launches;
     S->stats.alg_bytes = 12 * N;
     return QZGPU_NO_ERROR;

@@ -2,6 +2,8 @@
 // scratch storages, a pool of them for the single-block libbsc-style calls,
 // and host-buffer / device-buffer entry points.
 #include <algorithm>
+#include <cstdarg>
+#include <cstdio>
 #include <condition_variable>
 #include <cstdlib>
 #include <cstring>
@@ -22,6 +24,54 @@ int map_cuda_error(cudaError_t e) {
         case cudaErrorNoKernelImageForDevice: return QZGPU_GPU_NOT_SUPPORTED;
         default: return QZGPU_GPU_ERROR;
     }
+}
+
+bool debug_on() {
+    static int on = -1;
+    if (on < 0) {
+        const char* e = getenv("QZGPU_DEBUG");
+        on = (e && *e && *e != '0') ? 1 : 0;
+    }
+    return on == 1;
+}
+
+void debug_log(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    fprintf(stderr, "[qzgpu] ");
+    vfprintf(stderr, fmt, ap);
+    fprintf(stderr, "\n");
+    va_end(ap);
+}
+
+void debug_after(cudaStream_t st, const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) debug_log("%s: %s", what, cudaGetErrorString(e));
+}
+
+static const char* dump_dir() {
+    static const char* d = getenv("QZGPU_DUMP");
+    return (d && *d) ? d : nullptr;
+}
+
+bool dump_on() { return dump_dir() != nullptr; }
+
+void dump_array(const char* name, const void* dptr, size_t bytes, cudaStream_t st) {
+    static int seq = 0;
+    if (!dump_dir()) return;
+    std::vector<char> h(bytes);
+    cudaStreamSynchronize(st);
+    if (bytes && cudaMemcpy(h.data(), dptr, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        debug_log("dump %s: copy failed", name);
+        return;
+    }
+    char path[1024];
+    snprintf(path, sizeof(path), "%s/%04d_%s.bin", dump_dir(), seq++, name);
+    FILE* f = fopen(path, "wb");
+    if (!f) return;
+    if (bytes) fwrite(h.data(), 1, bytes, f);
+    fclose(f);
 }
 
 namespace {
