@@ -1,0 +1,379 @@
+"""Benchmark of the GB300 block-sorting stage (forward + inverse BWT).
+
+One step = forward BWT of every block of the workload followed by the inverse
+BWT of the result, device-resident inputs (the round trip is checked on the
+device after warm-up).  Default workload: one qz chunk of 2.5M synthetic
+150 bp reads split into qz's sequence / quality / header streams and cut into
+25 MiB blocks (about 33 blocks, 818 MB), all blocks in one batched call.
+
+Prints one JSON line (rank 0).  `--impl reference` times the CPU path instead
+(the C oracle over all host threads, one block per thread as qz runs libbsc
+under rayon), on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "BSC BWT fwd/inv MB/s on 1 GB300, batched+served p50/p99 vs plain kernel & CPU"
+FALLBACK_HBM_GBS = 6800.0
+
+
+# --------------------------------------------------------------------------- workload
+
+
+def make_workload(name: str, reads: int):
+    from qz_gb300 import synth
+
+    if name == "chunk":
+        blocks = synth.chunk_blocks(reads)
+        desc = f"one qz chunk: {reads} x 150 bp synthetic reads -> seq/qual/header streams, 25 MiB blocks"
+    elif name == "plain":
+        blocks = [("seq", synth.plain_block())]
+        desc = "one 24,999,900-byte sequence block (166,666 x 150 bp reads, 5 Mbp genome)"
+    elif name == "uneven":
+        blocks = synth.uneven_blocks(256)
+        desc = "256 blocks, sizes log-uniform 1 KB-25 MiB, 50% DNA / 30% quality / 20% header"
+    elif name == "repeat":
+        blocks = synth.repeat_blocks()
+        desc = "repeat-rich: 250 bp reads at 30x over 1 Mbp with 20% tandem repeats, one single-byte and one period-3 block"
+    else:
+        raise SystemExit(f"unknown config {name}")
+    return [b for _, b in blocks], [k for k, _ in blocks], desc
+
+
+# --------------------------------------------------------------------------- clocks
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (clocks and throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sms.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+# --------------------------------------------------------------------------- CPU path
+
+
+def cpu_sample(blocks, kinds, cores: int):
+    """Bounded sample: one block per host thread, kinds interleaved like the workload."""
+    order = sorted(range(len(blocks)), key=lambda i: (i % 3, i))
+    take = max(1, min(len(blocks), cores))
+    idx = sorted(order[:take])
+    return [blocks[i] for i in idx], [kinds[i] for i in idx]
+
+
+def time_cpu(sample, cores: int):
+    from oracle import oracle as O
+
+    O.build()
+    t0 = time.perf_counter()
+    us, idx = O.bwt_encode_batch(sample, threads=cores)
+    t1 = time.perf_counter()
+    back = O.bwt_decode_batch(us, idx, threads=cores)
+    t2 = time.perf_counter()
+    for a, b in zip(back, sample):
+        if not np.array_equal(a, b):
+            raise SystemExit("CPU round trip mismatch")
+    return t1 - t0, t2 - t1
+
+
+def cpu_desc(sample, kinds) -> str:
+    mb = sum(len(b) for b in sample) / 1e6
+    return f"{len(sample)} blocks ({mb:.1f} MB; " + ", ".join(f"{k}" for k in kinds) + ")"
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def run_reference(args, rank: int):
+    if rank != 0:
+        return
+    blocks, kinds, desc = make_workload(args.config, args.reads)
+    cores = os.cpu_count() or 1
+    sample, skinds = cpu_sample(blocks, kinds, cores)
+    nbytes = sum(len(b) for b in sample)
+    for _ in range(args.warmup):
+        time_cpu(sample, cores)
+    times = []
+    for _ in range(args.steps):
+        te, ti = time_cpu(sample, cores)
+        times.append(te + ti)
+    total = sum(times)
+    value = nbytes * args.steps / total / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "MB/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": desc, "sample_blocks": len(sample), "sample_bytes": nbytes},
+        "cpu_baseline": {"value": round(value, 3), "unit": "MB/s", "cores": cores, "kind": "port",
+                         "sample": cpu_desc(sample, skinds) + "; oracle CPU, not libbsc (libbsc is not in the "
+                                                             "reference tree)", "cpu": cpu_model()},
+        "e2e": {"value": round(value, 3), "unit": "MB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------- GPU path
+
+
+def load_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def load_traffic():
+    """Per-launch DRAM bytes of kernels from a committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def run_gpu(args, rank: int, world: int):
+    import torch
+
+    from qz_gb300 import bwt
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    blocks, kinds, desc = make_workload(args.config, args.reads)
+    sizes = [len(b) for b in blocks]
+    N = sum(sizes)
+    host = np.concatenate(blocks)
+    dev = torch.device("cuda", local)
+    d_T = torch.from_numpy(host).to(dev)
+    d_U = torch.empty_like(d_T)
+    d_R = torch.empty_like(d_T)
+    bwt.init()
+    st = bwt.Storage(N, len(blocks))
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    def step():
+        idx = st.encode_device(sizes, d_T.data_ptr(), d_U.data_ptr(), sptr)
+        fl = st.stats()["kernel_launches"]
+        st.decode_device(sizes, idx, d_U.data_ptr(), d_R.data_ptr(), sptr)
+        return idx, fl + st.stats()["kernel_launches"]
+
+    for _ in range(args.warmup):
+        idx, _ = step()
+    torch.cuda.synchronize(dev)
+    if not torch.equal(d_R, d_T):
+        raise SystemExit("GPU round trip mismatch")
+    fwd_stats = None
+
+    # ---- timed region (device-resident inputs, 818 MB > 126 MB L2)
+    clocks = ClockSampler(local)
+    st.profile(True)
+    st.profile_read(reset=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    time.sleep(0.3)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3 * args.steps + 1)]
+    launches = 0
+    ev[0].record(stream)
+    for k in range(args.steps):
+        idx = st.encode_device(sizes, d_T.data_ptr(), d_U.data_ptr(), sptr)
+        fwd_stats = st.stats()
+        launches += fwd_stats["kernel_launches"]
+        ev[3 * k + 1].record(stream)
+        st.decode_device(sizes, idx, d_U.data_ptr(), d_R.data_ptr(), sptr)
+        launches += st.stats()["kernel_launches"]
+        ev[3 * k + 2].record(stream)
+        ev[3 * k + 3].record(stream)
+    torch.cuda.synchronize(dev)
+    clk = clocks.stop()
+    if dist:
+        dist.barrier()
+    total_ms = ev[0].elapsed_time(ev[3 * args.steps])
+    fwd_ms = sum((ev[3 * k].elapsed_time(ev[3 * k + 1]) if k else ev[0].elapsed_time(ev[1])) for k in range(args.steps))
+    inv_ms = sum(ev[3 * k + 1].elapsed_time(ev[3 * k + 2]) for k in range(args.steps))
+    prof = st.profile_read(reset=True)
+    st.profile(False)
+    rounds_active = st.round_counts()
+    if dist:
+        t = torch.tensor([total_ms, fwd_ms, inv_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, fwd_ms, inv_ms = t.tolist()
+    value = world * N * args.steps / (total_ms / 1e3) / 1e6
+
+    # ---- roofline of the dominant kernel (event-timed inside the timed region)
+    peak, peak_kind = load_peak()
+    traffic = load_traffic()
+    kernels = []
+    for p in prof:
+        gbs = (p["alg_bytes"] / (p["ms"] / 1e3) / 1e9) if p["ms"] > 0 and p["alg_bytes"] > 0 else None
+        kernels.append({"name": p["name"], "launches": p["launches"], "ms": round(p["ms"], 3),
+                        "share": round(p["ms"] / max(sum(q["ms"] for q in prof), 1e-9), 4),
+                        "alg_gb_s": round(gbs, 1) if gbs else None})
+    top = prof[0] if prof else None
+    roof = None
+    if top:
+        per_launch_bytes = top["alg_bytes"] / max(top["launches"], 1)
+        avg_s = top["ms"] / max(top["launches"], 1) / 1e3
+        achieved = per_launch_bytes / avg_s / 1e9 if avg_s > 0 else 0.0
+        tr = traffic.get(top["name"])
+        roof = {"bound": "hbm", "kernel": top["name"], "achieved": round(achieved, 1), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                "alg_bytes_per_launch": int(per_launch_bytes),
+                "traffic": (tr.get("bytes_per_launch") if isinstance(tr, dict) else tr)}
+
+    # ---- end to end through the host-buffer C ABI (copies inside the timed region)
+    e2e = None
+    if not args.no_e2e:
+        us, ix = st.encode_batch(blocks)
+        st.decode_batch(us, ix)
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            us, ix = st.encode_batch(blocks)
+            back = st.decode_batch(us, ix)
+        t1 = time.perf_counter()
+        if not all(np.array_equal(a, b) for a, b in zip(back, blocks)):
+            raise SystemExit("host round trip mismatch")
+        e2e_s = t1 - t0
+        if dist:
+            t = torch.tensor([e2e_s], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": round(world * N * args.steps / e2e_s / 1e6, 3), "unit": "MB/s",
+               "h2d_bytes_per_step": 2 * N, "d2h_bytes_per_step": 2 * N,
+               "api": "qzgpu_bwt_encode_batch + qzgpu_bwt_decode_batch (host buffers)"}
+
+    # ---- CPU baseline on a bounded sample (rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        sample, skinds = cpu_sample(blocks, kinds, cores)
+        te, ti = time_cpu(sample, cores)
+        cpu = {"value": round(sum(len(b) for b in sample) / (te + ti) / 1e6, 3), "unit": "MB/s", "cores": cores,
+               "kind": "port", "sample": cpu_desc(sample, skinds) + "; forward+inverse, oracle CPU, not libbsc",
+               "fwd_mb_s": round(sum(len(b) for b in sample) / te / 1e6, 3),
+               "inv_mb_s": round(sum(len(b) for b in sample) / ti / 1e6, 3), "cpu": cpu_model()}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "MB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded reads of the workload's shape; no public dataset)",
+            "config": {"workload": desc, "blocks": len(blocks), "bytes": N,
+                       "l2": "inputs larger than L2 (workload bytes and scratch exceed 126 MB)",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "step": "forward BWT of all blocks + inverse BWT of the result"},
+            "fwd_mb_s": round(world * N * args.steps / (fwd_ms / 1e3) / 1e6, 3),
+            "inv_mb_s": round(world * N * args.steps / (inv_ms / 1e3) / 1e6, 3),
+            "rounds": fwd_stats["rounds"] if fwd_stats else None,
+            "active_per_round": rounds_active,
+            "gpu_launches": launches,
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "kernels": kernels[:12],
+        }
+        print(json.dumps(line), flush=True)
+    st.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="chunk", choices=["chunk", "plain", "uneven", "repeat"])
+    ap.add_argument("--reads", type=int, default=2_500_000)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+    else:
+        run_gpu(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -135,6 +135,25 @@ typedef struct qzgpu_stats {
 } qzgpu_stats;
 int qzgpu_storage_last_stats(const qzgpu_storage *storage, qzgpu_stats *out);
 
+/* Suffixes sorted per round of the last forward call on a storage (entry 0:
+ * the initial sort of every suffix; entry r: suffixes still in groups before
+ * doubling round r).  Copies up to `max` entries; returns how many exist. */
+int qzgpu_storage_round_counts(const qzgpu_storage *storage, long long *active, int max);
+
+/* Per-kernel timing of later calls on a storage: when enabled, every launch
+ * is bracketed by CUDA events on the stream it runs on.  Diagnostic only; no
+ * counterpart in libbsc. */
+typedef struct qzgpu_kernel_time {
+    char name[32];
+    int launches;
+    double ms;              /* summed event-measured duration */
+    long long alg_bytes;    /* summed algorithmic HBM bytes of those launches */
+} qzgpu_kernel_time;
+int qzgpu_storage_profile(qzgpu_storage *storage, int enable);
+/* Copies up to `max` records (largest total time first); returns the number
+ * of kernels recorded.  reset != 0 clears the records afterwards. */
+int qzgpu_storage_profile_read(qzgpu_storage *storage, qzgpu_kernel_time *out, int max, int reset);
+
 #ifdef __cplusplus
 }
 #endif

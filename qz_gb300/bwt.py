@@ -107,6 +107,22 @@ class Storage:
         return {"rounds": s.rounds, "kernel_launches": s.kernel_launches, "active_total": s.active_total,
                 "alg_bytes": s.alg_bytes}
 
+    def round_counts(self) -> list[int]:
+        """Suffixes sorted per round of the last forward call (entry 0 = all)."""
+        buf = (ctypes.c_longlong * 64)()
+        n = check(self._lib.qzgpu_storage_round_counts(self._h, buf, 64), "qzgpu_storage_round_counts")
+        return [int(buf[i]) for i in range(min(n, 64))]
+
+    def profile(self, enable: bool = True) -> None:
+        """Times every later launch on this storage with CUDA events."""
+        check(self._lib.qzgpu_storage_profile(self._h, int(enable)), "qzgpu_storage_profile")
+
+    def profile_read(self, reset: bool = True) -> list[dict]:
+        buf = (native.KernelTime * 64)()
+        n = check(self._lib.qzgpu_storage_profile_read(self._h, buf, 64, int(reset)), "qzgpu_storage_profile_read")
+        return [{"name": buf[i].name.decode(), "launches": buf[i].launches, "ms": buf[i].ms,
+                 "alg_bytes": buf[i].alg_bytes} for i in range(min(n, 64))]
+
     def _ptr_arrays(self, ins, outs):
         nb = len(ins)
         inp = (_u8p * max(nb, 1))(*[_ptr(b) for b in ins])

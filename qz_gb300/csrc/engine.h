@@ -5,7 +5,9 @@
 #include <stdint.h>
 
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "common.cuh"
@@ -14,22 +16,22 @@ namespace qz {
 
 // Segment classes of the per-round sort (by group length).
 constexpr int kSmallMax = 16;    // one thread, register bitonic network
-constexpr int kMedMax = 4096;    // one CTA, shared-memory bitonic sort
-constexpr int kRT = 4096;        // tile of the segmented radix sort (larger groups)
+constexpr int kMedMax = 512;     // one warp, register bitonic sort across lanes
+constexpr int kRT = 2048;        // tile of the segmented radix sort (larger groups)
 constexpr int kInitTile = 4096;  // text positions per tile of the per-block passes
-constexpr int kSplitGrid = 1024; // fixed grid of the split phases
 constexpr int kMaxRounds = 40;   // prefix doubling needs <= 31 rounds for n < 2^31
 
 // Device counters (int32 slots of Storage::counters).
 enum Counter {
     CNT_ACTIVE = 0,  // suffixes still in non-singleton groups (two slots: 0 and 6,
                      // a split reads one and writes the other)
-    CNT_SMALL = 1,   // descriptor counts per class
-    CNT_MED = 2,
+    CNT_MED = 2,     // descriptor counts of the listed classes
     CNT_LARGE = 3,
     CNT_LTILES = 4,  // tiles of the large-group radix sort
     CNT_LHIST = 5,   // histogram entries of the large-group radix sort (256 per tile)
     CNT_ACTIVE_ALT = 6,
+    CNT_MED_ELEMS = 8,  // slots covered by each listed class
+    CNT_LARGE_ELEMS = 9,
     CNT_SLOTS = 16,
 };
 
@@ -37,16 +39,22 @@ struct FwdBuffers {
     int* SA;
     int* R;
     uint32_t* key;
-    int* W[2];
-    int* P[2];
-    int* G[2];
+    int* W[2];   // compact slots: suffix
+    int* G[2];   // compact slots: group rank (SA position of the group's first slot)
     uint32_t* wsk[2];
     int* wsv[2];
-    int2* list[3];
-    uint32_t* ltc;     // large: tiles per segment -> tile base
-    uint32_t* llen;    // large: length per segment -> workspace base
+    int2* list_med;
+    int2* list_large;
+    uint32_t* ltc;     // large: tiles per group -> tile base
+    uint32_t* llen;    // large: length per group -> workspace base
     uint32_t* ltbase;
     uint32_t* lwbase;
+    uint32_t* p_surv;  // split: per 256-slot warp tile
+    int* p_sub;
+    int* p_grp;
+    uint32_t* c_surv;  // split: per scan chunk
+    int* c_sub;
+    int* c_grp;
 };
 
 struct InvBuffers {
@@ -74,7 +82,6 @@ struct Storage {
     uint32_t* hist = nullptr;     // per-tile digit histograms (large sort / LF build)
     size_t hist_cap = 0;          // uint32 entries
     uint32_t* partial = nullptr;  // scan partials
-    int* split_part = nullptr;    // split phase partials (2 * kSplitGrid)
     int* counters = nullptr;
     DevStatus* status = nullptr;
 
@@ -105,6 +112,24 @@ struct Storage {
 
     std::mutex mu;
     qzgpu_stats stats{};
+    int launches = 0;  // kernels launched by the current call
+
+    // optional per-kernel timing (CUDA events around each launch)
+    struct ProfRec {
+        const char* name;
+        cudaEvent_t a, b;
+        long long bytes;
+    };
+    struct ProfAgg {
+        int launches = 0;
+        double ms = 0;
+        long long bytes = 0;
+    };
+    bool profile = false;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_next = 0;
+    std::vector<ProfRec> prof_pending;
+    std::map<std::string, ProfAgg> prof;
     std::vector<int> rounds_active;  // active suffixes per round of the last forward call
 };
 
@@ -134,6 +159,17 @@ void debug_log(const char* fmt, ...);
 // batches to <dir>/<seq>_<name>.bin for offline inspection.
 bool dump_on();
 void dump_array(const char* name, const void* dptr, size_t bytes, cudaStream_t st);
+cudaEvent_t prof_begin(Storage* S, cudaStream_t st);
+void prof_end(Storage* S, cudaStream_t st, const char* name, long long bytes, cudaEvent_t a);
+void prof_flush(Storage* S);  // after the stream is idle: fold pending records in
+// Launch wrapper: counts the launch, times it when profiling, checks it in debug mode.
+#define QZ_LAUNCH(S, st, name, bytes, ...)                     \
+    do {                                                       \
+        cudaEvent_t _qz_a = ::qz::prof_begin(S, st);           \
+        __VA_ARGS__;                                           \
+        ::qz::prof_end(S, st, name, (long long)(bytes), _qz_a); \
+        QZ_DBG(st, name);                                      \
+    } while (0)
 #define QZ_DBG(st, what)                              \
     do {                                              \
         if (::qz::debug_on()) ::qz::debug_after(st, what); \

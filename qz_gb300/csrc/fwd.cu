@@ -21,20 +21,20 @@
 //      each group, split, repeat until every group is a singleton;
 //   5. extract U and the primary index (libsais convention).
 //
-// Groups are kept in a compact work list in SA order (slot arrays P = SA
-// position, W = suffix, G = group head).  Per round each group is sorted by
-// the kernel of its size class: <= 16 in registers, <= 4096 in shared memory,
+// Groups are kept in a compact work list in SA order (slot arrays W =
+// suffix, G = group rank); a slot's SA position is G plus its offset in the
+// group.  Per round each group is sorted by the kernel of its size class:
+// <= 16 slots in registers (found from G, no list), <= 4096 in shared memory,
 // larger ones by a segmented LSD radix sort (8-bit digits, warp match-based
-// stable ranking, shared-memory staged scatter).
+// stable ranking, shared-memory staged scatter).  The secondary-key gather is
+// fused into the sorts.
 #include "engine.h"
 #include "scan.cuh"
 
 namespace qz {
 
-constexpr int kSplitItems = 8;
-constexpr int kSplitTile = kThreads * kSplitItems;
-constexpr int kRItems = kRT / kThreads;  // 16 elements per thread in a radix tile
-constexpr int kRWarpSpan = kRT / kWarps; // 512 contiguous elements per warp
+constexpr int kRItems = kRT / kThreads;  // elements per thread in a radix tile
+constexpr int kRWarpSpan = kRT / kWarps; // contiguous elements per warp in a radix tile
 
 // ------------------------------------------------------------------ per-block alphabet
 
@@ -119,56 +119,163 @@ __global__ void __launch_bounds__(kThreads) k_init_keys(const uint8_t* __restric
     }
 }
 
+// ------------------------------------------------------------------ rank gather
+
+// Secondary key of suffix x in doubling round `round` (h = K_b << round):
+// R[x+h] + h + 1 when x+h is inside the block, else the remaining length
+// (n_b - i), which is <= h and orders the shorter suffix first.  round < 0:
+// the key was computed from the text (initial sort) and is read from `key`.
+struct GatherArgs {
+    const int* R;
+    const int* off;
+    int nb;
+    const int* Kb;
+    int round;
+};
+
+struct BlockSpan {
+    int bs, n;
+    long long h;
+};
+
+__device__ __forceinline__ BlockSpan block_span(const GatherArgs& g, int x) {
+    int b = block_of(g.off, g.nb, x);
+    BlockSpan s;
+    s.bs = __ldg(g.off + b);
+    s.n = __ldg(g.off + b + 1) - s.bs;
+    s.h = g.round >= 31 ? (long long)s.n : ((long long)__ldg(g.Kb + b) << g.round);
+    if (s.h > s.n) s.h = s.n;
+    return s;
+}
+
+__device__ __forceinline__ uint32_t rank_key(const GatherArgs& g, const BlockSpan& s, int x) {
+    int i = x - s.bs;
+    if ((long long)i + s.h < s.n) return (uint32_t)__ldg(g.R + x + (int)s.h) + (uint32_t)s.h + 1u;
+    return (uint32_t)(s.n - i);
+}
+
 // ------------------------------------------------------------------ group sorts
 
 __device__ __forceinline__ unsigned long long pack_kv(uint32_t k, int v) {
     return ((unsigned long long)k << 32) | (uint32_t)v;
 }
 
-__global__ void __launch_bounds__(kThreads) k_sort_small(const int2* __restrict__ list,
-                                                         const int* __restrict__ d_count,
-                                                         uint32_t* __restrict__ key, int* __restrict__ W) {
-    int cnt = *d_count;
-    for (int i = blockIdx.x * kThreads + threadIdx.x; i < cnt; i += gridDim.x * kThreads) {
-        int2 d = list[i];
-        int s = d.x, len = d.y;
-        if (len == 2) {
-            uint32_t k0 = key[s], k1 = key[s + 1];
-            if (k1 < k0) {
-                int w0 = W[s], w1 = W[s + 1];
-                key[s] = k1;
-                key[s + 1] = k0;
-                W[s] = w1;
-                W[s + 1] = w0;
-            }
-            continue;
-        }
-        unsigned long long v[kSmallMax];
+template <int M>
+__device__ __forceinline__ void bitonic_regs(unsigned long long (&v)[M]) {
 #pragma unroll
-        for (int j = 0; j < kSmallMax; ++j) v[j] = j < len ? pack_kv(key[s + j], W[s + j]) : ~0ull;
+    for (int k = 2; k <= M; k <<= 1) {
 #pragma unroll
-        for (int k = 2; k <= kSmallMax; k <<= 1) {
+        for (int jj = k >> 1; jj > 0; jj >>= 1) {
 #pragma unroll
-            for (int jj = k >> 1; jj > 0; jj >>= 1) {
-#pragma unroll
-                for (int a = 0; a < kSmallMax; ++a) {
-                    int l = a ^ jj;
-                    if (l > a) {
-                        bool up = (a & k) == 0;
-                        unsigned long long x = v[a], y = v[l];
-                        bool sw = up ? (x > y) : (x < y);
-                        v[a] = sw ? y : x;
-                        v[l] = sw ? x : y;
-                    }
+            for (int a = 0; a < M; ++a) {
+                int l = a ^ jj;
+                if (l > a) {
+                    bool up = (a & k) == 0;
+                    unsigned long long x = v[a], y = v[l];
+                    bool sw = up ? (x > y) : (x < y);
+                    v[a] = sw ? y : x;
+                    v[l] = sw ? x : y;
                 }
             }
         }
+    }
+}
+
+template <int M>
+__device__ __forceinline__ void sort_group_regs(int s, int len, uint32_t* key, int* W) {
+    unsigned long long v[M];
 #pragma unroll
-        for (int j = 0; j < kSmallMax; ++j) {
-            if (j < len) {
-                key[s + j] = (uint32_t)(v[j] >> 32);
-                W[s + j] = (int)(uint32_t)v[j];
+    for (int j = 0; j < M; ++j) v[j] = j < len ? pack_kv(key[s + j], W[s + j]) : ~0ull;
+    bitonic_regs<M>(v);
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+        if (j < len) {
+            key[s + j] = (uint32_t)(v[j] >> 32);
+            W[s + j] = (int)(uint32_t)v[j];
+        }
+    }
+}
+
+// Groups of 2..16 slots: the thread of a group's first slot finds the group
+// from the group-rank array G and sorts it in registers.  Longer groups are
+// left to the listed sorts.
+__global__ void __launch_bounds__(kThreads) k_sort_small(const int* __restrict__ d_A, const int* __restrict__ G,
+                                                         uint32_t* __restrict__ key, int* __restrict__ W) {
+    int A = *d_A;
+    for (int k = blockIdx.x * kThreads + threadIdx.x; k < A; k += gridDim.x * kThreads) {
+        int g = G[k];
+        if (k > 0 && G[k - 1] == g) continue;
+        int L = 1;
+        while (L <= kSmallMax && k + L < A && G[k + L] == g) ++L;
+        if (L > kSmallMax || L < 2) continue;
+        if (L == 2) {
+            uint32_t k0 = key[k], k1 = key[k + 1];
+            if (k1 < k0) {
+                int w0 = W[k], w1 = W[k + 1];
+                key[k] = k1;
+                key[k + 1] = k0;
+                W[k] = w1;
+                W[k + 1] = w0;
             }
+        } else if (L <= 4) {
+            sort_group_regs<4>(k, L, key, W);
+        } else if (L <= 8) {
+            sort_group_regs<8>(k, L, key, W);
+        } else {
+            sort_group_regs<16>(k, L, key, W);
+        }
+    }
+}
+
+// Groups of 17..512 slots: one warp per listed group, bitonic sort across
+// lanes in registers (element e = lane + 32 r, M registers per lane).
+template <int M>
+__device__ __forceinline__ void warp_sort_group(int s, int len, uint32_t* key, int* W) {
+    const int ln = (int)lane_id();
+    unsigned long long v[M];
+#pragma unroll
+    for (int r = 0; r < M; ++r) {
+        int e = ln + 32 * r;
+        v[r] = e < len ? pack_kv(key[s + e], W[s + e]) : ~0ull;
+    }
+#pragma unroll
+    for (int k = 2; k <= 32 * M; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+                const int jr = j / 32;
+#pragma unroll
+                for (int r = 0; r < M; ++r) {
+                    int pr = r ^ jr;
+                    if (pr > r) {
+                        int e = ln + 32 * r;
+                        bool up = (e & k) == 0;
+                        unsigned long long x = v[r], y = v[pr];
+                        bool sw = up ? (x > y) : (x < y);
+                        v[r] = sw ? y : x;
+                        v[pr] = sw ? x : y;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < M; ++r) {
+                    int e = ln + 32 * r;
+                    unsigned long long y = __shfl_xor_sync(0xffffffffu, v[r], j);
+                    bool lower = (ln & j) == 0;
+                    bool up = (e & k) == 0;
+                    unsigned long long mn = v[r] < y ? v[r] : y;
+                    unsigned long long mx = v[r] < y ? y : v[r];
+                    v[r] = (lower == up) ? mn : mx;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < M; ++r) {
+        int e = ln + 32 * r;
+        if (e < len) {
+            key[s + e] = (uint32_t)(v[r] >> 32);
+            W[s + e] = (int)(uint32_t)v[r];
         }
     }
 }
@@ -176,40 +283,31 @@ __global__ void __launch_bounds__(kThreads) k_sort_small(const int2* __restrict_
 __global__ void __launch_bounds__(kThreads) k_sort_medium(const int2* __restrict__ list,
                                                           const int* __restrict__ d_count,
                                                           uint32_t* __restrict__ key, int* __restrict__ W) {
-    __shared__ unsigned long long buf[kMedMax];
     int cnt = *d_count;
-    for (int i = blockIdx.x; i < cnt; i += gridDim.x) {
+    int nwarps = gridDim.x * kWarps;
+    for (int i = blockIdx.x * kWarps + (int)warp_id(); i < cnt; i += nwarps) {
         int2 d = list[i];
-        int s = d.x, len = d.y;
-        int np = 2;
-        while (np < len) np <<= 1;
-        for (int j = threadIdx.x; j < np; j += kThreads) buf[j] = j < len ? pack_kv(key[s + j], W[s + j]) : ~0ull;
-        __syncthreads();
-        for (int k = 2; k <= np; k <<= 1) {
-            for (int jj = k >> 1; jj > 0; jj >>= 1) {
-                for (int a = threadIdx.x; a < np; a += kThreads) {
-                    int l = a ^ jj;
-                    if (l > a) {
-                        unsigned long long x = buf[a], y = buf[l];
-                        bool up = (a & k) == 0;
-                        if (up ? (x > y) : (x < y)) {
-                            buf[a] = y;
-                            buf[l] = x;
-                        }
-                    }
-                }
-                __syncthreads();
-            }
-        }
-        for (int j = threadIdx.x; j < len; j += kThreads) {
-            key[s + j] = (uint32_t)(buf[j] >> 32);
-            W[s + j] = (int)(uint32_t)buf[j];
-        }
-        __syncthreads();
+        if (d.y <= 32) warp_sort_group<1>(d.x, d.y, key, W);
+        else if (d.y <= 64) warp_sort_group<2>(d.x, d.y, key, W);
+        else if (d.y <= 128) warp_sort_group<4>(d.x, d.y, key, W);
+        else if (d.y <= 256) warp_sort_group<8>(d.x, d.y, key, W);
+        else warp_sort_group<16>(d.x, d.y, key, W);
     }
 }
 
-// Large groups: tiles per group and workspace layout (groups back to back).
+// All active slots: the secondary key of each suffix (one rank gathered).
+__global__ void __launch_bounds__(kThreads) k_gather(const int* __restrict__ d_A, const int* __restrict__ W,
+                                                     uint32_t* __restrict__ key, GatherArgs ga) {
+    int A = *d_A;
+    for (int k = blockIdx.x * kThreads + threadIdx.x; k < A; k += gridDim.x * kThreads) {
+        int x = __ldcs(W + k);
+        BlockSpan bsp = block_span(ga, x);
+        __stcs(key + k, rank_key(ga, bsp, x));
+    }
+}
+
+// ------------------------------------------------------------------ large groups: segmented LSD radix sort
+
 __global__ void __launch_bounds__(kThreads) k_large_prep(const int2* __restrict__ list,
                                                          const int* __restrict__ d_count,
                                                          uint32_t* __restrict__ tcount,
@@ -270,11 +368,13 @@ __global__ void __launch_bounds__(kThreads) k_large_up(LargeArgs a, const uint32
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_large_down(LargeArgs a, const uint32_t* __restrict__ hist,
-                                                         const uint32_t* __restrict__ srck,
-                                                         const int* __restrict__ srcv, int src_compact,
-                                                         uint32_t* __restrict__ dstk, int* __restrict__ dstv,
-                                                         int dst_compact, int shift) {
+// One stable 8-bit digit pass over a tile: warp match-based ranks, scatter
+// staged in shared memory so that runs of one digit leave as coalesced writes.
+__global__ void __launch_bounds__(kThreads, 3) k_large_down(LargeArgs a, const uint32_t* __restrict__ hist,
+                                                            const uint32_t* __restrict__ srck,
+                                                            const int* __restrict__ srcv, int src_compact,
+                                                            uint32_t* __restrict__ dstk, int* __restrict__ dstv,
+                                                            int dst_compact, int shift) {
     __shared__ uint32_t skey[kRT];
     __shared__ int sval[kRT];
     __shared__ uint32_t wcnt[kWarps][256];
@@ -296,15 +396,12 @@ __global__ void __launch_bounds__(kThreads) k_large_down(LargeArgs a, const uint
         int m = (d.y + kRT - 1) / kRT;
         int srcbase = (src_compact ? d.x : (int)a.wbase[s]) + j * kRT;
         int cnt = min(kRT, d.y - j * kRT);
-        uint32_t kk[kRItems];
-        int vv[kRItems];
         uint32_t rk[kRItems];
 #pragma unroll
         for (int it = 0; it < kRItems; ++it) {
             int i = (int)w * kRWarpSpan + it * 32 + (int)ln;
             bool valid = i < cnt;
             uint32_t kv = valid ? srck[srcbase + i] : 0u;
-            int vl = valid ? srcv[srcbase + i] : 0;
             unsigned dg = valid ? (kv >> shift) & 255u : 256u;
             unsigned peers = __match_any_sync(0xffffffffu, dg);
             unsigned before = __popc(peers & lt_mask);
@@ -312,8 +409,6 @@ __global__ void __launch_bounds__(kThreads) k_large_down(LargeArgs a, const uint
             __syncwarp();
             if (valid && before == 0) wcnt[w][dg] = prev + __popc(peers);
             __syncwarp();
-            kk[it] = kv;
-            vv[it] = vl;
             rk[it] = prev + before;
         }
         __syncthreads();
@@ -337,10 +432,11 @@ __global__ void __launch_bounds__(kThreads) k_large_down(LargeArgs a, const uint
         for (int it = 0; it < kRItems; ++it) {
             int i = (int)w * kRWarpSpan + it * 32 + (int)ln;
             if (i < cnt) {
-                unsigned dg = (kk[it] >> shift) & 255u;
+                uint32_t kv = srck[srcbase + i];
+                unsigned dg = (kv >> shift) & 255u;
                 uint32_t lp = dig_off[dg] + wcnt[w][dg] + rk[it];
-                skey[lp] = kk[it];
-                sval[lp] = vv[it];
+                skey[lp] = kv;
+                sval[lp] = srcv[srcbase + i];
             }
         }
         __syncthreads();
@@ -356,152 +452,156 @@ __global__ void __launch_bounds__(kThreads) k_large_down(LargeArgs a, const uint
 }
 
 // ------------------------------------------------------------------ split into groups
+//
+// After a sort, slot k (compact, SA order) holds suffix W[k] of group G[k]
+// (the group's rank = SA position of its first slot) with sort key key[k].
+// A subgroup starts where G or key changes.  Each warp owns a tile of 256
+// consecutive slots (lane l holds slots base + 32 i + l); per-tile partials
+// (survivors, last subgroup head, last group head) are scanned across tiles
+// so the apply pass needs no block-level synchronisation:
+//   slot SA position  P = G + (k - first slot of the group)
+//   new rank          = G + (first slot of the subgroup - first slot of the group)
+// Singleton subgroups are final (SA[P] = suffix); the others are compacted,
+// in order, into the next round's slot arrays.
+
+constexpr int kWT = 256;  // slots per warp tile
+constexpr int kWI = kWT / 32;
 
 struct SplitArgs {
     const int* A;      // active slots of this split
     int* A_next;       // receives the survivor count
     const uint32_t* key;
     const int* G;
-    const int* P;  // null: slot k is SA position k (first split)
     const int* W;
     int* R;
     int* SA;
-    int* Pn;
     int* Wn;
     int* Gn;
-    int2* list0;
-    int2* list1;
-    int2* list2;
+    int2* list_med;
+    int2* list_large;
     int* counters;
-    int* part_surv;  // [kSplitGrid]
-    int* part_head;  // [kSplitGrid]
+    uint32_t* p_surv;  // per warp tile; exclusive prefix after the partial scan
+    int* p_sub;
+    int* p_grp;
+    int write_all;     // first split: no previous ranks to keep
 };
 
-struct SplitItems {
-    uint32_t k[kSplitItems];
-    int g[kSplitItems];
-    bool head[kSplitItems];
-    bool nhead[kSplitItems];
+struct WarpTile {
+    uint32_t k[kWI];
+    int g[kWI];
+    bool valid[kWI], gh[kWI], sh[kWI], nsh[kWI];
 };
 
-// Loads this thread's kSplitItems consecutive slots starting at k0 (< hi) and
-// computes group-head flags for each and for its successor.
-__device__ __forceinline__ void split_load(const SplitArgs& a, int A, int k0, int hi, SplitItems& it) {
-    if (k0 + kSplitItems <= hi) {
-        const uint4* kp = reinterpret_cast<const uint4*>(a.key + k0);
-        const int4* gp = reinterpret_cast<const int4*>(a.G + k0);
-        uint4 k01 = kp[0], k23 = kp[1];
-        int4 g01 = gp[0], g23 = gp[1];
-        it.k[0] = k01.x; it.k[1] = k01.y; it.k[2] = k01.z; it.k[3] = k01.w;
-        it.k[4] = k23.x; it.k[5] = k23.y; it.k[6] = k23.z; it.k[7] = k23.w;
-        it.g[0] = g01.x; it.g[1] = g01.y; it.g[2] = g01.z; it.g[3] = g01.w;
-        it.g[4] = g23.x; it.g[5] = g23.y; it.g[6] = g23.z; it.g[7] = g23.w;
-    } else {
+__device__ __forceinline__ void wt_load(const SplitArgs& a, int A, int base, WarpTile& t) {
+    const unsigned ln = lane_id();
 #pragma unroll
-        for (int i = 0; i < kSplitItems; ++i) {
-            int k = k0 + i;
-            it.k[i] = k < hi ? a.key[k] : 0u;
-            it.g[i] = k < hi ? a.G[k] : 0;
+    for (int i = 0; i < kWI; ++i) {
+        int kk = base + 32 * i + (int)ln;
+        t.valid[i] = kk < A;
+        t.k[i] = t.valid[i] ? a.key[kk] : 0u;
+        t.g[i] = t.valid[i] ? a.G[kk] : -1;
+    }
+    uint32_t pk = 0, nk = 0;
+    int pg = -1, ng = -1;
+    if (base > 0) {
+        pk = a.key[base - 1];
+        pg = a.G[base - 1];
+    }
+    if (base + kWT < A) {
+        nk = a.key[base + kWT];
+        ng = a.G[base + kWT];
+    }
+#pragma unroll
+    for (int i = 0; i < kWI; ++i) {
+        uint32_t prevk = __shfl_up_sync(0xffffffffu, t.k[i], 1);
+        int prevg = __shfl_up_sync(0xffffffffu, t.g[i], 1);
+        uint32_t lk = __shfl_sync(0xffffffffu, t.k[i > 0 ? i - 1 : 0], 31);
+        int lg = __shfl_sync(0xffffffffu, t.g[i > 0 ? i - 1 : 0], 31);
+        if (ln == 0) {
+            prevk = i > 0 ? lk : pk;
+            prevg = i > 0 ? lg : pg;
         }
-    }
-    uint32_t pk = 0;
-    int pg = 0;
-    if (k0 > 0) {
-        pk = a.key[k0 - 1];
-        pg = a.G[k0 - 1];
+        int kk = base + 32 * i + (int)ln;
+        t.gh[i] = t.valid[i] && (kk == 0 || prevg != t.g[i]);
+        t.sh[i] = t.valid[i] && (t.gh[i] || prevk != t.k[i]);
     }
 #pragma unroll
-    for (int i = 0; i < kSplitItems; ++i) {
-        int k = k0 + i;
-        if (k == 0) it.head[i] = true;
-        else if (i == 0) it.head[i] = it.g[0] != pg || it.k[0] != pk;
-        else it.head[i] = it.g[i] != it.g[i - 1] || it.k[i] != it.k[i - 1];
-    }
-#pragma unroll
-    for (int i = 0; i < kSplitItems; ++i) {
-        int k = k0 + i;
-        if (k >= hi) {
-            it.nhead[i] = true;
-        } else if (k + 1 >= A) {
-            it.nhead[i] = true;
-        } else if (i + 1 < kSplitItems && k + 1 < hi) {
-            it.nhead[i] = it.head[i + 1];
-        } else {
-            it.nhead[i] = a.G[k + 1] != it.g[i] || a.key[k + 1] != it.k[i];
+    for (int i = 0; i < kWI; ++i) {
+        uint32_t nxk = __shfl_down_sync(0xffffffffu, t.k[i], 1);
+        int nxg = __shfl_down_sync(0xffffffffu, t.g[i], 1);
+        uint32_t fk = __shfl_sync(0xffffffffu, t.k[i + 1 < kWI ? i + 1 : i], 0);
+        int fg = __shfl_sync(0xffffffffu, t.g[i + 1 < kWI ? i + 1 : i], 0);
+        if (ln == 31) {
+            nxk = i + 1 < kWI ? fk : nk;
+            nxg = i + 1 < kWI ? fg : ng;
         }
+        int kk = base + 32 * i + (int)ln;
+        t.nsh[i] = kk + 1 >= A || nxg != t.g[i] || nxk != t.k[i];
     }
 }
 
 __global__ void __launch_bounds__(kThreads) k_split_count(SplitArgs a) {
-    __shared__ uint32_t shs[kWarps + 1];
-    __shared__ int shm[kWarps + 1];
     int A = *a.A;
-    int lo, hi;
-    chunk_range(A, gridDim.x, blockIdx.x, kSplitTile, &lo, &hi);
-    uint32_t surv = 0;
-    int lasthead = -1;
-    for (int base = lo; base < hi; base += kSplitTile) {
-        int k0 = base + threadIdx.x * kSplitItems;
-        if (k0 < hi) {
-            SplitItems it;
-            split_load(a, A, k0, hi, it);
+    int ntiles = (A + kWT - 1) / kWT;
+    int nwarps = gridDim.x * kWarps;
+    for (int tile = blockIdx.x * kWarps + (int)warp_id(); tile < ntiles; tile += nwarps) {
+        int base = tile * kWT;
+        WarpTile t;
+        wt_load(a, A, base, t);
+        uint32_t surv = 0;
+        int sub = -1, grp = -1;
 #pragma unroll
-            for (int i = 0; i < kSplitItems; ++i) {
-                int k = k0 + i;
-                if (k < hi) {
-                    surv += (it.head[i] && it.nhead[i]) ? 0u : 1u;
-                    if (it.head[i]) lasthead = k;
-                }
-            }
+        for (int i = 0; i < kWI; ++i) {
+            int kk = base + 32 * i + (int)lane_id();
+            surv += (t.valid[i] && !(t.sh[i] && t.nsh[i])) ? 1u : 0u;
+            if (t.sh[i]) sub = kk;
+            if (t.gh[i]) grp = kk;
         }
-    }
-    uint32_t tot;
-    block_excl_sum(surv, shs, &tot);
-    int mx;
-    block_incl_max(lasthead, shm, &mx);
-    if (threadIdx.x == 0) {
-        a.part_surv[blockIdx.x] = (int)tot;
-        a.part_head[blockIdx.x] = mx;
+        surv = warp_sum(surv);
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            sub = max(sub, __shfl_xor_sync(0xffffffffu, sub, d));
+            grp = max(grp, __shfl_xor_sync(0xffffffffu, grp, d));
+        }
+        if (lane_id() == 0) {
+            a.p_surv[tile] = surv;
+            a.p_sub[tile] = sub;
+            a.p_grp[tile] = grp;
+        }
     }
 }
 
-// One CTA: exclusive sum of survivors and exclusive max of group heads over
-// the split chunks; new active count; resets the descriptor counters.
-__global__ void __launch_bounds__(kThreads) k_split_top(SplitArgs a) {
+// Exclusive scan of the per-tile partials (sum of survivors, max of the two
+// head positions), reduce-then-scan over kScanGrid chunks.
+__global__ void __launch_bounds__(kThreads) k_pscan_reduce(SplitArgs a, uint32_t* __restrict__ cs,
+                                                           int* __restrict__ cm1, int* __restrict__ cm2) {
     __shared__ uint32_t shs[kWarps + 1];
     __shared__ int shm[kWarps + 1];
-    uint32_t carry = 0;
-    int mcarry = -1;
-    for (int base = 0; base < kSplitGrid; base += kThreads) {
-        int i = base + threadIdx.x;
-        uint32_t v = (uint32_t)a.part_surv[i];
-        int h = a.part_head[i];
-        uint32_t tot;
-        uint32_t ex = block_excl_sum(v, shs, &tot);
-        int mtot;
-        int inc = block_incl_max(h, shm, &mtot);
-        int exm = __shfl_up_sync(0xffffffffu, inc, 1);
-        __shared__ int lastw[kWarps];
-        if (lane_id() == 31) lastw[warp_id()] = inc;
-        __syncthreads();
-        if (lane_id() == 0) exm = warp_id() == 0 ? -1 : lastw[warp_id() - 1];
-        __syncthreads();
-        a.part_surv[i] = (int)(carry + ex);
-        a.part_head[i] = max(mcarry, exm);
-        carry += tot;
-        mcarry = max(mcarry, mtot);
+    int n = (*a.A + kWT - 1) / kWT;
+    int lo, hi;
+    chunk_range(n, gridDim.x, blockIdx.x, kThreads, &lo, &hi);
+    uint32_t s = 0;
+    int m1 = -1, m2 = -1;
+    for (int i = lo + threadIdx.x; i < hi; i += kThreads) {
+        s += a.p_surv[i];
+        m1 = max(m1, a.p_sub[i]);
+        m2 = max(m2, a.p_grp[i]);
     }
+    uint32_t ts;
+    block_excl_sum(s, shs, &ts);
+    int t1, t2;
+    block_incl_max(m1, shm, &t1);
+    block_incl_max(m2, shm, &t2);
     if (threadIdx.x == 0) {
-        *a.A_next = (int)carry;
-        a.counters[CNT_SMALL] = 0;
-        a.counters[CNT_MED] = 0;
-        a.counters[CNT_LARGE] = 0;
+        cs[blockIdx.x] = ts;
+        cm1[blockIdx.x] = t1;
+        cm2[blockIdx.x] = t2;
     }
 }
 
 __device__ __forceinline__ int block_excl_max(int v, int* sh, int* total) {
-    int inc = block_incl_max(v, sh, total);
     __shared__ int lastw[kWarps];
+    int inc = block_incl_max(v, sh, total);
     int ex = __shfl_up_sync(0xffffffffu, inc, 1);
     if (lane_id() == 31) lastw[warp_id()] = inc;
     __syncthreads();
@@ -510,121 +610,122 @@ __device__ __forceinline__ int block_excl_max(int v, int* sh, int* total) {
     return ex;
 }
 
-__global__ void __launch_bounds__(kThreads) k_split_apply(SplitArgs a) {
+__global__ void __launch_bounds__(kThreads) k_pscan_top(SplitArgs a, uint32_t* __restrict__ cs,
+                                                        int* __restrict__ cm1, int* __restrict__ cm2, int n) {
     __shared__ uint32_t shs[kWarps + 1];
     __shared__ int shm[kWarps + 1];
-    __shared__ unsigned long long shl[kWarps + 1];
-    __shared__ int lbase[3];
-    int A = *a.A;
-    int lo, hi;
-    chunk_range(A, gridDim.x, blockIdx.x, kSplitTile, &lo, &hi);
-    uint32_t surv_carry = (uint32_t)a.part_surv[blockIdx.x];
-    int head_carry = a.part_head[blockIdx.x];
-    for (int base = lo; base < hi; base += kSplitTile) {
-        int k0 = base + threadIdx.x * kSplitItems;
-        SplitItems it;
-        bool any = k0 < hi;
-        if (any) split_load(a, A, k0, hi, it);
-        uint32_t mysurv = 0;
-        int myhead = -1;
-        if (any) {
-#pragma unroll
-            for (int i = 0; i < kSplitItems; ++i) {
-                int k = k0 + i;
-                if (k < hi) {
-                    mysurv += (it.head[i] && it.nhead[i]) ? 0u : 1u;
-                    if (it.head[i]) myhead = k;
-                }
-            }
+    uint32_t carry = 0;
+    int c1 = -1, c2 = -1;
+    for (int base = 0; base < n; base += kThreads) {
+        int i = base + threadIdx.x;
+        uint32_t v = i < n ? cs[i] : 0u;
+        int m1 = i < n ? cm1[i] : -1, m2 = i < n ? cm2[i] : -1;
+        uint32_t tot;
+        uint32_t ex = block_excl_sum(v, shs, &tot);
+        int t1, t2;
+        int e1 = block_excl_max(m1, shm, &t1);
+        int e2 = block_excl_max(m2, shm, &t2);
+        if (i < n) {
+            cs[i] = carry + ex;
+            cm1[i] = max(c1, e1);
+            cm2[i] = max(c2, e2);
         }
-        uint32_t stot;
-        uint32_t sex = block_excl_sum(mysurv, shs, &stot);
-        int mtot;
-        int hex = block_excl_max(myhead, shm, &mtot);
-        int kg = max(head_carry, hex);
-        uint32_t dest = surv_carry + sex;
-        // group heads and class counts of group tails
-        int kgs[kSplitItems];
-        unsigned long long cls_cnt = 0;
-        if (any) {
-#pragma unroll
-            for (int i = 0; i < kSplitItems; ++i) {
-                int k = k0 + i;
-                if (k < hi) {
-                    if (it.head[i]) kg = k;
-                    kgs[i] = kg;
-                    bool single = it.head[i] && it.nhead[i];
-                    if (!single && it.nhead[i]) {
-                        int L = k - kg + 1;
-                        int c = L <= kSmallMax ? 0 : (L <= kMedMax ? 1 : 2);
-                        cls_cnt += 1ull << (16 * c);
-                    }
-                }
-            }
-        }
-        unsigned long long ctot;
-        unsigned long long cex = block_excl_sum(cls_cnt, shl, &ctot);
-        if (threadIdx.x == 0) {
-            lbase[0] = (ctot & 0xffff) ? atomicAdd(&a.counters[CNT_SMALL], (int)(ctot & 0xffff)) : 0;
-            lbase[1] = ((ctot >> 16) & 0xffff) ? atomicAdd(&a.counters[CNT_MED], (int)((ctot >> 16) & 0xffff)) : 0;
-            lbase[2] = ((ctot >> 32) & 0xffff) ? atomicAdd(&a.counters[CNT_LARGE], (int)((ctot >> 32) & 0xffff)) : 0;
-        }
-        __syncthreads();
-        if (any) {
-            int lp[3] = {lbase[0] + (int)(cex & 0xffff), lbase[1] + (int)((cex >> 16) & 0xffff),
-                         lbase[2] + (int)((cex >> 32) & 0xffff)};
-            int2* lists[3] = {a.list0, a.list1, a.list2};
-#pragma unroll
-            for (int i = 0; i < kSplitItems; ++i) {
-                int k = k0 + i;
-                if (k < hi) {
-                    int kgi = kgs[i];
-                    int rank = a.P ? a.P[kgi] : kgi;
-                    int w = a.W[k];
-                    int pk = a.P ? a.P[k] : k;
-                    a.R[w] = rank;
-                    bool single = it.head[i] && it.nhead[i];
-                    if (single) {
-                        a.SA[pk] = w;
-                    } else {
-                        a.Pn[dest] = pk;
-                        a.Wn[dest] = w;
-                        a.Gn[dest] = rank;
-                        if (it.nhead[i]) {
-                            int L = k - kgi + 1;
-                            int c = L <= kSmallMax ? 0 : (L <= kMedMax ? 1 : 2);
-                            lists[c][lp[c]++] = make_int2((int)dest - L + 1, L);
-                        }
-                        ++dest;
-                    }
-                }
-            }
-        }
-        // carry to the next tile of this chunk
-        surv_carry += stot;
-        head_carry = max(head_carry, mtot);
-        __syncthreads();
+        carry += tot;
+        c1 = max(c1, t1);
+        c2 = max(c2, t2);
+    }
+    if (threadIdx.x == 0) {
+        *a.A_next = (int)carry;
+        a.counters[CNT_MED] = 0;
+        a.counters[CNT_LARGE] = 0;
+        a.counters[CNT_MED_ELEMS] = 0;
+        a.counters[CNT_LARGE_ELEMS] = 0;
     }
 }
 
-// ------------------------------------------------------------------ rounds
+__global__ void __launch_bounds__(kThreads) k_pscan_apply(SplitArgs a, const uint32_t* __restrict__ cs,
+                                                          const int* __restrict__ cm1,
+                                                          const int* __restrict__ cm2) {
+    __shared__ uint32_t shs[kWarps + 1];
+    __shared__ int shm[kWarps + 1];
+    int n = (*a.A + kWT - 1) / kWT;
+    int lo, hi;
+    chunk_range(n, gridDim.x, blockIdx.x, kThreads, &lo, &hi);
+    uint32_t carry = cs[blockIdx.x];
+    int c1 = cm1[blockIdx.x], c2 = cm2[blockIdx.x];
+    for (int base = lo; base < hi; base += kThreads) {
+        int i = base + threadIdx.x;
+        bool ok = i < hi;
+        uint32_t v = ok ? a.p_surv[i] : 0u;
+        int m1 = ok ? a.p_sub[i] : -1, m2 = ok ? a.p_grp[i] : -1;
+        uint32_t tot;
+        uint32_t ex = block_excl_sum(v, shs, &tot);
+        int t1, t2;
+        int e1 = block_excl_max(m1, shm, &t1);
+        int e2 = block_excl_max(m2, shm, &t2);
+        if (ok) {
+            a.p_surv[i] = carry + ex;
+            a.p_sub[i] = max(c1, e1);
+            a.p_grp[i] = max(c2, e2);
+        }
+        carry += tot;
+        c1 = max(c1, t1);
+        c2 = max(c2, t2);
+    }
+}
 
-__global__ void __launch_bounds__(kThreads) k_gather(const int* __restrict__ d_A, const int* __restrict__ W,
-                                                     const int* __restrict__ R, const int* __restrict__ off,
-                                                     int nb, const int* __restrict__ Kb, int round,
-                                                     uint32_t* __restrict__ key) {
-    int A = *d_A;
-    for (int k = blockIdx.x * kThreads + threadIdx.x; k < A; k += gridDim.x * kThreads) {
-        int x = W[k];
-        int b = block_of(off, nb, x);
-        int bs = __ldg(off + b), n = __ldg(off + b + 1) - bs;
-        long long h = round >= 31 ? (long long)n : ((long long)__ldg(Kb + b) << round);
-        if (h > n) h = n;
-        int i = x - bs;
-        uint32_t kv;
-        if ((long long)i + h < n) kv = (uint32_t)R[x + (int)h] + (uint32_t)h + 1u;
-        else kv = (uint32_t)(n - i);
-        key[k] = kv;
+__global__ void __launch_bounds__(kThreads) k_split_apply(SplitArgs a) {
+    int A = *a.A;
+    int ntiles = (A + kWT - 1) / kWT;
+    int nwarps = gridDim.x * kWarps;
+    const unsigned ln = lane_id();
+    const unsigned lt_mask = (1u << ln) - 1u;
+    for (int tile = blockIdx.x * kWarps + (int)warp_id(); tile < ntiles; tile += nwarps) {
+        int base = tile * kWT;
+        WarpTile t;
+        wt_load(a, A, base, t);
+        uint32_t dest = a.p_surv[tile];
+        int csub = a.p_sub[tile], cgrp = a.p_grp[tile];
+#pragma unroll
+        for (int i = 0; i < kWI; ++i) {
+            int kk = base + 32 * i + (int)ln;
+            int ks = warp_incl_max(t.sh[i] ? kk : -1);
+            int kg = warp_incl_max(t.gh[i] ? kk : -1);
+            ks = max(ks, csub);
+            kg = max(kg, cgrp);
+            csub = __shfl_sync(0xffffffffu, ks, 31);
+            cgrp = __shfl_sync(0xffffffffu, kg, 31);
+            bool single = t.sh[i] && t.nsh[i];
+            bool surv = t.valid[i] && !single;
+            unsigned m = __ballot_sync(0xffffffffu, surv);
+            uint32_t d = dest + __popc(m & lt_mask);
+            dest += __popc(m);
+            if (t.valid[i]) {
+                int w = __ldcs(a.W + kk);
+                int g = t.g[i];
+                int rank = g + (ks - kg);
+                if (a.write_all || rank != g) a.R[w] = rank;
+                if (single) {
+                    a.SA[g + (kk - kg)] = w;
+                } else {
+                    __stcs(a.Wn + d, w);
+                    __stcs(a.Gn + d, rank);
+                    if (t.nsh[i]) {
+                        int L = kk - ks + 1;
+                        if (L > kSmallMax) {
+                            int2 dsc = make_int2((int)d - L + 1, L);
+                            if (L <= kMedMax) {
+                                a.list_med[atomicAdd(&a.counters[CNT_MED], 1)] = dsc;
+                                atomicAdd(&a.counters[CNT_MED_ELEMS], L);
+                            } else {
+                                a.list_large[atomicAdd(&a.counters[CNT_LARGE], 1)] = dsc;
+                                atomicAdd(&a.counters[CNT_LARGE_ELEMS], L);
+                            }
+                        }
+                    }
+                }
+            }
+        }
     }
 }
 
@@ -662,12 +763,6 @@ __global__ void __launch_bounds__(kThreads) k_extract(int N, const int* __restri
 
 namespace {
 
-struct Launch {
-    cudaStream_t st;
-    int sms;
-    int* launches;
-};
-
 int grid_for(long long work, int per_cta, int cap) {
     long long g = (work + per_cta - 1) / per_cta;
     if (g < 1) g = 1;
@@ -675,47 +770,44 @@ int grid_for(long long work, int per_cta, int cap) {
     return (int)g;
 }
 
-// Sorts every listed group (key, W) in place in compact slot space.
-void sort_groups(Storage* S, const int* host_counts, uint32_t* key, int* W, const Launch& L) {
+// Sorts every group (key, W) in place in compact slot space.  hc: host copy
+// of the counters (list lengths, slots per class); A: active slots.
+void sort_groups(Storage* S, const int* hc, int A, const int* d_A, uint32_t* key, int* W, const int* G,
+                 cudaStream_t st) {
     FwdBuffers& f = S->f;
     int* cnt = S->counters;
-    int nsm = host_counts[CNT_SMALL], nmd = host_counts[CNT_MED], nlg = host_counts[CNT_LARGE];
-    if (nsm > 0) {
-        k_sort_small<<<grid_for(nsm, kThreads, L.sms * 16), kThreads, 0, L.st>>>(f.list[0], cnt + CNT_SMALL, key, W);
-        QZ_DBG(L.st, "k_sort_small");
-        ++*L.launches;
-    }
-    if (nmd > 0) {
-        k_sort_medium<<<grid_for(nmd, 1, L.sms * 4), kThreads, 0, L.st>>>(f.list[1], cnt + CNT_MED, key, W);
-        QZ_DBG(L.st, "k_sort_medium");
-        ++*L.launches;
-    }
+    const int sms = S->sms;
+    int nmd = hc[CNT_MED], nlg = hc[CNT_LARGE];
+    long long small_el = (long long)A - hc[CNT_MED_ELEMS] - hc[CNT_LARGE_ELEMS];
+    // every slot: group rank read; small groups: key and suffix read and written
+    QZ_LAUNCH(S, st, "k_sort_small", 4ll * A + 16ll * small_el,
+              k_sort_small<<<grid_for(A, kThreads, sms * 16), kThreads, 0, st>>>(d_A, G, key, W));
+    if (nmd > 0)
+        QZ_LAUNCH(S, st, "k_sort_medium", 16ll * hc[CNT_MED_ELEMS] + 8ll * nmd,
+                  k_sort_medium<<<grid_for(nmd, kWarps, sms * 16), kThreads, 0, st>>>(f.list_med, cnt + CNT_MED,
+                                                                                      key, W));
     if (nlg > 0) {
-        k_large_prep<<<grid_for(nlg, kThreads, L.sms * 4), kThreads, 0, L.st>>>(f.list[2], cnt + CNT_LARGE, f.ltc,
-                                                                                 f.llen);
-        QZ_DBG(L.st, "k_large_prep");
-        ++*L.launches;
-        scan_exclusive(f.ltc, f.ltbase, 0, cnt + CNT_LARGE, S->partial, (uint32_t*)(cnt + CNT_LTILES), L.st,
-                       L.launches);
-        scan_exclusive(f.llen, f.lwbase, 0, cnt + CNT_LARGE, S->partial, nullptr, L.st, L.launches);
-        LargeArgs la{f.list[2], cnt + CNT_LARGE, f.ltbase, f.lwbase, cnt + CNT_LTILES, cnt + CNT_LHIST};
-        // upper bound of tiles: every large group is > kMedMax >= kRT long
-        int grid = L.sms * 4;
+        long long le = hc[CNT_LARGE_ELEMS];
+        QZ_LAUNCH(S, st, "k_large_prep", 16ll * nlg,
+                  k_large_prep<<<grid_for(nlg, kThreads, sms * 4), kThreads, 0, st>>>(f.list_large, cnt + CNT_LARGE,
+                                                                                      f.ltc, f.llen));
+        scan_exclusive(S, f.ltc, f.ltbase, 0, cnt + CNT_LARGE, (uint32_t*)(cnt + CNT_LTILES), st);
+        scan_exclusive(S, f.llen, f.lwbase, 0, cnt + CNT_LARGE, nullptr, st);
+        LargeArgs la{f.list_large, cnt + CNT_LARGE, f.ltbase, f.lwbase, cnt + CNT_LTILES, cnt + CNT_LHIST};
+        int grid = sms * 6;
         const uint32_t* sk[4] = {key, f.wsk[0], f.wsk[1], f.wsk[0]};
         const int* sv[4] = {W, f.wsv[0], f.wsv[1], f.wsv[0]};
         uint32_t* dk[4] = {f.wsk[0], f.wsk[1], f.wsk[0], key};
         int* dv[4] = {f.wsv[0], f.wsv[1], f.wsv[0], W};
         for (int pass = 0; pass < 4; ++pass) {
             int shift = 8 * pass;
-            k_large_up<<<grid, kThreads, 0, L.st>>>(la, sk[pass], pass == 0, shift, S->hist);
-            QZ_DBG(L.st, "k_large_up");
-            ++*L.launches;
+            QZ_LAUNCH(S, st, "k_large_up", 4 * le,
+                      k_large_up<<<grid, kThreads, 0, st>>>(la, sk[pass], pass == 0, shift, S->hist));
             // histogram entries = 256 * tiles (count on device)
-            scan_exclusive(S->hist, S->hist, 0, cnt + CNT_LHIST, S->partial, nullptr, L.st, L.launches);
-            k_large_down<<<grid, kThreads, 0, L.st>>>(la, S->hist, sk[pass], sv[pass], pass == 0, dk[pass],
-                                                      dv[pass], pass == 3, shift);
-            QZ_DBG(L.st, "k_large_down");
-            ++*L.launches;
+            scan_exclusive(S, S->hist, S->hist, 0, cnt + CNT_LHIST, nullptr, st);
+            QZ_LAUNCH(S, st, "k_large_down", 16 * le,
+                      k_large_down<<<grid, kThreads, 0, st>>>(la, S->hist, sk[pass], sv[pass], pass == 0, dk[pass],
+                                                              dv[pass], pass == 3, shift));
         }
     }
 }
@@ -733,27 +825,31 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
     if (N > S->cap_bytes) return QZGPU_BAD_PARAMETER;
     S->stats = qzgpu_stats{};
     S->rounds_active.clear();
+    S->launches = 0;
     for (int b = 0; b < nb; ++b) idx[b] = n[b] <= 1 ? n[b] : -1;
     if (N == 0) return QZGPU_NO_ERROR;
-
-    int launches = 0;
-    Launch L{st, S->sms, &launches};
     FwdBuffers& f = S->f;
 
-    // ---- host tables (pinned) -> device in one copy
+    // ---- host tables (pinned) -> device
     std::vector<int> off(nb + 1, 0);
     for (int b = 0; b < nb; ++b) off[b + 1] = off[b] + n[b];
     std::vector<int2> tiles;
     tiles.reserve((size_t)(N / kInitTile) + nb + 1);
     for (int b = 0; b < nb; ++b)
         for (int s = off[b]; s < off[b + 1]; s += kInitTile) tiles.push_back(make_int2(b, s));
-    std::vector<int2> l0, l1, l2;
+    // initial groups = blocks; blocks of <= kSmallMax bytes need no list
+    std::vector<int2> l1, l2;
+    int cnt0[CNT_SLOTS] = {0};
     for (int b = 0; b < nb; ++b) {
-        if (n[b] < 2) continue;
+        if (n[b] <= kSmallMax) continue;
         int2 dsc = make_int2(off[b], n[b]);
-        if (n[b] <= kSmallMax) l0.push_back(dsc);
-        else if (n[b] <= kMedMax) l1.push_back(dsc);
-        else l2.push_back(dsc);
+        if (n[b] <= kMedMax) {
+            l1.push_back(dsc);
+            cnt0[CNT_MED_ELEMS] += n[b];
+        } else {
+            l2.push_back(dsc);
+            cnt0[CNT_LARGE_ELEMS] += n[b];
+        }
     }
     int aux_total = 0;
     std::vector<int> aoff(nb, 0);
@@ -763,9 +859,8 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
             if (aux_rate[b] > 0 && n[b] > 0) aux_total += (n[b] - 1) / aux_rate[b];
         }
     }
-    // pinned layout: off | tiles | lists | counters | aux_rate | aux_off
-    size_t need = sizeof(int) * (nb + 1) + sizeof(int2) * (tiles.size() + l0.size() + l1.size() + l2.size()) +
-                  sizeof(int) * CNT_SLOTS + sizeof(int) * 2 * nb + 64;
+    size_t need = sizeof(int) * (nb + 1) + sizeof(int2) * (tiles.size() + l1.size() + l2.size()) +
+                  sizeof(int) * CNT_SLOTS + sizeof(int) * 2 * nb + 64 * 8;
     if (need > S->pin_tab_bytes || aux_total > 64 * S->cap_blocks) return QZGPU_BAD_PARAMETER;
     char* p = S->pin_tab;
     auto put = [&](const void* src, size_t bytes) {
@@ -776,27 +871,22 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
     };
     char* h_off = put(off.data(), sizeof(int) * off.size());
     char* h_tiles = put(tiles.data(), sizeof(int2) * tiles.size());
-    char* h_l0 = put(l0.data(), sizeof(int2) * l0.size());
     char* h_l1 = put(l1.data(), sizeof(int2) * l1.size());
     char* h_l2 = put(l2.data(), sizeof(int2) * l2.size());
-    int cnt0[CNT_SLOTS] = {0};
     cnt0[CNT_ACTIVE] = (int)N;
-    cnt0[CNT_SMALL] = (int)l0.size();
     cnt0[CNT_MED] = (int)l1.size();
     cnt0[CNT_LARGE] = (int)l2.size();
     char* h_cnt = put(cnt0, sizeof(cnt0));
     char* h_ar = aux_rate ? put(aux_rate, sizeof(int) * nb) : nullptr;
     char* h_ao = aux_rate ? put(aoff.data(), sizeof(int) * nb) : nullptr;
-    cudaError_t e;
+    cudaError_t e = cudaSuccess;
     auto h2d = [&](void* dst, const char* src, size_t bytes) {
         if (bytes && e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
     };
-    e = cudaSuccess;
     h2d(S->blk_off, h_off, sizeof(int) * off.size());
     h2d(S->tiles, h_tiles, sizeof(int2) * tiles.size());
-    h2d(f.list[0], h_l0, sizeof(int2) * l0.size());
-    h2d(f.list[1], h_l1, sizeof(int2) * l1.size());
-    h2d(f.list[2], h_l2, sizeof(int2) * l2.size());
+    h2d(f.list_med, h_l1, sizeof(int2) * l1.size());
+    h2d(f.list_large, h_l2, sizeof(int2) * l2.size());
     h2d(S->counters, h_cnt, sizeof(cnt0));
     if (aux_rate) {
         h2d(S->blk_aux_rate, h_ar, sizeof(int) * nb);
@@ -809,115 +899,122 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
 
     // ---- alphabet, initial keys
     int ntiles = (int)tiles.size();
-    k_block_hist<<<ntiles, kThreads, 0, st>>>(d_T, S->tiles, S->blk_off, S->blk_hist);
-    QZ_DBG(st, "k_block_hist");
-    k_block_alpha<<<nb, kThreads, 0, st>>>(S->blk_hist, S->blk_code, S->blk_K, S->blk_sigma);
-    QZ_DBG(st, "k_block_alpha");
-    k_init_keys<<<ntiles, kThreads, 0, st>>>(d_T, S->tiles, S->blk_off, S->blk_code, S->blk_K, S->blk_sigma, f.key,
-                                             f.W[0], f.G[0]);
-    QZ_DBG(st, "k_init_keys");
-    launches += 3;
-
+    QZ_LAUNCH(S, st, "k_block_hist", N,
+              k_block_hist<<<ntiles, kThreads, 0, st>>>(d_T, S->tiles, S->blk_off, S->blk_hist));
+    QZ_LAUNCH(S, st, "k_block_alpha", 1280ll * nb,
+              k_block_alpha<<<nb, kThreads, 0, st>>>(S->blk_hist, S->blk_code, S->blk_K, S->blk_sigma));
+    // reads T once, writes key, W and G
+    QZ_LAUNCH(S, st, "k_init_keys", 13 * N,
+              k_init_keys<<<ntiles, kThreads, 0, st>>>(d_T, S->tiles, S->blk_off, S->blk_code, S->blk_K,
+                                                       S->blk_sigma, f.key, f.W[0], f.G[0]));
     const bool dump = dump_on() && N <= (1 << 20);
     if (dump) {
         dump_array("init_key", f.key, 4 * N, st);
         dump_array("init_W", f.W[0], 4 * N, st);
         dump_array("init_G", f.G[0], 4 * N, st);
-        dump_array("blk_K", S->blk_K, 4 * nb, st);
-        dump_array("blk_sigma", S->blk_sigma, 4 * nb, st);
     }
-    // ---- initial sort (groups = blocks) and split
-    int hc[CNT_SLOTS];
-    memcpy(hc, cnt0, sizeof(hc));
-    sort_groups(S, hc, f.key, f.W[0], L);
+    int cur = 0;
+    int act = CNT_ACTIVE;  // counter slot holding the current active count
+    GatherArgs ga{f.R, S->blk_off, nb, S->blk_K, -1};
+    // ---- initial sort (groups = blocks)
+    sort_groups(S, cnt0, (int)N, S->counters + act, f.key, f.W[0], f.G[0], st);
     if (dump) {
         dump_array("sorted_key", f.key, 4 * N, st);
         dump_array("sorted_W", f.W[0], 4 * N, st);
     }
-    int cur = 0;
-    int act = CNT_ACTIVE;  // counter slot holding the current active count
-    auto split = [&](const int* P) {
+    auto split = [&](long long A, bool first) {
         SplitArgs a;
         a.A = S->counters + act;
         a.A_next = S->counters + (act ^ (CNT_ACTIVE ^ CNT_ACTIVE_ALT));
         a.key = f.key;
         a.G = f.G[cur];
-        a.P = P;
         a.W = f.W[cur];
         a.R = f.R;
         a.SA = f.SA;
-        a.Pn = f.P[cur ^ 1];
         a.Wn = f.W[cur ^ 1];
         a.Gn = f.G[cur ^ 1];
-        a.list0 = f.list[0];
-        a.list1 = f.list[1];
-        a.list2 = f.list[2];
+        a.list_med = f.list_med;
+        a.list_large = f.list_large;
         a.counters = S->counters;
-        a.part_surv = S->split_part;
-        a.part_head = S->split_part + kSplitGrid;
-        k_split_count<<<kSplitGrid, kThreads, 0, st>>>(a);
-        QZ_DBG(st, "k_split_count");
-        k_split_top<<<1, kThreads, 0, st>>>(a);
-        QZ_DBG(st, "k_split_top");
-        k_split_apply<<<kSplitGrid, kThreads, 0, st>>>(a);
-        QZ_DBG(st, "k_split_apply");
-        launches += 3;
+        a.p_surv = f.p_surv;
+        a.p_sub = f.p_sub;
+        a.p_grp = f.p_grp;
+        a.write_all = first ? 1 : 0;
+        int grid = grid_for((A + kWT - 1) / kWT, kWarps, S->sms * 8);
+        long long tiles_n = (A + kWT - 1) / kWT;
+        // count: key and group rank of every slot; 12 bytes of partials per tile
+        QZ_LAUNCH(S, st, "k_split_count", 8 * A + 12 * tiles_n, k_split_count<<<grid, kThreads, 0, st>>>(a));
+        QZ_LAUNCH(S, st, "k_pscan_reduce", 12 * tiles_n,
+                  k_pscan_reduce<<<kScanGrid, kThreads, 0, st>>>(a, f.c_surv, f.c_sub, f.c_grp));
+        QZ_LAUNCH(S, st, "k_pscan_top", 24ll * kScanGrid,
+                  k_pscan_top<<<1, kThreads, 0, st>>>(a, f.c_surv, f.c_sub, f.c_grp, kScanGrid));
+        QZ_LAUNCH(S, st, "k_pscan_apply", 24 * tiles_n,
+                  k_pscan_apply<<<kScanGrid, kThreads, 0, st>>>(a, f.c_surv, f.c_sub, f.c_grp));
+        // apply: key, group, suffix in; rank out where it changed; then the
+        // suffix either leaves (SA) or is compacted (2 words); fixed up below
+        QZ_LAUNCH(S, st, first ? "k_split_apply_first" : "k_split_apply", 12 * A + 12 * tiles_n,
+                  k_split_apply<<<grid, kThreads, 0, st>>>(a));
         cur ^= 1;
         act ^= CNT_ACTIVE ^ CNT_ACTIVE_ALT;
     };
-    split(nullptr);
     auto dump_split = [&]() {
         if (!dump) return;
         dump_array("split_counters", S->counters, 4 * CNT_SLOTS, st);
         dump_array("split_R", f.R, 4 * N, st);
         dump_array("split_SA", f.SA, 4 * N, st);
-        dump_array("split_P", f.P[cur], 4 * N, st);
         dump_array("split_W", f.W[cur], 4 * N, st);
         dump_array("split_G", f.G[cur], 4 * N, st);
-        dump_array("split_list0", f.list[0], 8 * N / 2, st);
-        dump_array("split_list1", f.list[1], 8 * (N / 17 + 1), st);
-        dump_array("split_part", S->split_part, 4 * 2 * kSplitGrid, st);
     };
+    split(N, true);
     dump_split();
     S->rounds_active.push_back((int)N);
 
     int* hcnt = S->pin_rd;
     int round = 0;
+    long long A_prev = N;
+    bool first_split = true;
     for (;;) {
         e = cudaMemcpyAsync(hcnt, S->counters, sizeof(int) * CNT_SLOTS, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return map_cuda_error(e);
         int A = hcnt[act];
+        // the last split wrote A survivors (8 B) and A_prev - A suffix-array
+        // entries (4 B), and 4 B of rank per slot whose rank it changed (all on
+        // the first split; bounded by the slots otherwise)
+        if (S->profile && !S->prof_pending.empty() && S->prof_pending.back().name &&
+            strncmp(S->prof_pending.back().name, "k_split_apply", 13) == 0)
+            S->prof_pending.back().bytes += 8ll * A + 4ll * (A_prev - A) + (first_split ? 4ll * A_prev : 0);
+        first_split = false;
         if (A == 0) break;
         if (debug_on())
-            debug_log("round %d: active %d small %d medium %d large %d", round, A, hcnt[CNT_SMALL], hcnt[CNT_MED],
-                      hcnt[CNT_LARGE]);
+            debug_log("round %d: active %d medium %d/%d large %d/%d", round, A, hcnt[CNT_MED], hcnt[CNT_MED_ELEMS],
+                      hcnt[CNT_LARGE], hcnt[CNT_LARGE_ELEMS]);
         if (round >= kMaxRounds) {
             if (debug_on()) debug_log("no convergence after %d rounds", round);
             return QZGPU_GPU_ERROR;
         }
         S->rounds_active.push_back(A);
-        k_gather<<<grid_for(A, kThreads, S->sms * 16), kThreads, 0, st>>>(S->counters + act, f.W[cur], f.R,
-                                                                          S->blk_off, nb, S->blk_K, round, f.key);
-        QZ_DBG(st, "k_gather");
-        ++launches;
-        if (dump) dump_array("gather_key", f.key, 4 * (size_t)A, st);
-        sort_groups(S, hcnt, f.key, f.W[cur], L);
+        ga.round = round;
+        // reads the suffix, gathers one rank, writes the key
+        QZ_LAUNCH(S, st, "k_gather", 12ll * A,
+                  k_gather<<<grid_for(A, kThreads, S->sms * 16), kThreads, 0, st>>>(S->counters + act, f.W[cur],
+                                                                                    f.key, ga));
+        sort_groups(S, hcnt, A, S->counters + act, f.key, f.W[cur], f.G[cur], st);
         if (dump) {
             dump_array("rsorted_key", f.key, 4 * (size_t)A, st);
             dump_array("rsorted_W", f.W[cur], 4 * (size_t)A, st);
         }
-        split(f.P[cur]);
+        split(A, false);
         dump_split();
+        A_prev = A;
         ++round;
     }
 
-    // ---- U and primary indexes
-    k_extract<<<grid_for(N, kThreads, S->sms * 16), kThreads, 0, st>>>(
-        (int)N, f.SA, f.R, d_T, S->blk_off, nb, d_U, S->blk_idx, aux_rate ? S->blk_aux_rate : nullptr,
-        S->blk_aux_off, S->aux, S->status);
-    QZ_DBG(st, "k_extract");
-    ++launches;
+    // ---- U and primary indexes: SA read, one byte gathered, one written
+    QZ_LAUNCH(S, st, "k_extract", 6 * N,
+              k_extract<<<grid_for(N, kThreads, S->sms * 16), kThreads, 0, st>>>(
+                  (int)N, f.SA, f.R, d_T, S->blk_off, nb, d_U, S->blk_idx, aux_rate ? S->blk_aux_rate : nullptr,
+                  S->blk_aux_off, S->aux, S->status));
     DevStatus& hst = *reinterpret_cast<DevStatus*>(S->pin_rd + S->cap_blocks + 64);
     e = cudaMemcpyAsync(hcnt, S->blk_idx, sizeof(int) * nb, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&hst, S->status, sizeof(hst), cudaMemcpyDeviceToHost, st);
@@ -925,6 +1022,7 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
         e = cudaMemcpyAsync(aux_out, S->aux, sizeof(int) * aux_total, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return map_cuda_error(e);
+    prof_flush(S);
     if (hst.error) {
         if (debug_on()) debug_log("device status %d at %d detail %lld", hst.error, hst.where, hst.detail);
         return hst.error;
@@ -941,7 +1039,7 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
     long long active_sum = 0;
     for (int a : S->rounds_active) active_sum += a;
     S->stats.rounds = round;
-    S->stats.kernel_launches = launches;
+    S->stats.kernel_launches = S->launches;
     S->stats.active_total = active_sum;
     S->stats.alg_bytes = 15 * N + 28 * active_sum;
     return QZGPU_NO_ERROR;

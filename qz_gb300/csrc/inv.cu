@@ -234,8 +234,8 @@ int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t*
     }
     if (N > S->cap_bytes) return QZGPU_BAD_PARAMETER;
     S->stats = qzgpu_stats{};
+    S->launches = 0;
     if (N == 0) return QZGPU_NO_ERROR;
-    int launches = 0;
     const int stride_log2 = 5;  // rulers every 32 rows
     const int stride = 1 << stride_log2;
 
@@ -286,39 +286,36 @@ int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t*
     InvArgs a{d_U, S->blk_off, S->blk_idx, S->blk_tbase, S->blk_aux_off, S->tiles, v.LF, stride_log2, S->status};
     int ntiles = (int)tiles.size();
     int hist_len = tbase[nb] * 256;
-    k_inv_up<<<ntiles, kThreads, 0, st>>>(a, S->hist);
-    QZ_DBG(st, "k_inv_up");
-    scan_exclusive(S->hist, S->hist, hist_len, nullptr, S->partial, nullptr, st, &launches);
-    k_inv_down<<<ntiles, kThreads, 0, st>>>(a, S->hist);
-    QZ_DBG(st, "k_inv_down");
-    launches += 2;
+    long long rows = N + nb;
+    // U read once for the histogram, once for the ranks; LF written once
+    QZ_LAUNCH(S, st, "k_inv_up", N, k_inv_up<<<ntiles, kThreads, 0, st>>>(a, S->hist));
+    scan_exclusive(S, S->hist, S->hist, hist_len, nullptr, nullptr, st);
+    QZ_LAUNCH(S, st, "k_inv_down", 5 * N, k_inv_down<<<ntiles, kThreads, 0, st>>>(a, S->hist));
     RulerArgs r{v.rtiles, v.rnext[0], v.rdist[0], v.rlen};
     int nrt = (int)rtiles.size();
-    k_inv_walk1<<<nrt, kThreads, 0, st>>>(a, r);
-    QZ_DBG(st, "k_inv_walk1");
-    ++launches;
-    int it = 0;
+    // every row's LF entry read once; 12 bytes per ruler written
+    QZ_LAUNCH(S, st, "k_inv_walk1", 4 * rows + 12ll * Mtot, k_inv_walk1<<<nrt, kThreads, 0, st>>>(a, r));
     int cur = 0;
     int jgrid = (int)std::min<long long>(((long long)Mtot + kThreads - 1) / kThreads, (long long)S->sms * 16);
     for (long long span = 1; span < maxM + 1; span <<= 1) {
-        k_inv_jump<<<jgrid, kThreads, 0, st>>>(Mtot, v.rnext[cur], v.rdist[cur], v.rnext[cur ^ 1], v.rdist[cur ^ 1]);
-        QZ_DBG(st, "k_inv_jump");
-        ++launches;
+        QZ_LAUNCH(S, st, "k_inv_jump", 24ll * Mtot,
+                  k_inv_jump<<<jgrid, kThreads, 0, st>>>(Mtot, v.rnext[cur], v.rdist[cur], v.rnext[cur ^ 1],
+                                                          v.rdist[cur ^ 1]));
         cur ^= 1;
-        ++it;
     }
-    k_inv_walk2<<<nrt, kThreads, 0, st>>>(a, r, v.rnext[cur], v.rdist[cur], S->hist, d_T);
-    QZ_DBG(st, "k_inv_walk2");
-    ++launches;
+    // every row's LF entry read again and one output byte written per row
+    QZ_LAUNCH(S, st, "k_inv_walk2", 4 * rows + N + 12ll * Mtot,
+              k_inv_walk2<<<nrt, kThreads, 0, st>>>(a, r, v.rnext[cur], v.rdist[cur], S->hist, d_T));
     DevStatus* hst = reinterpret_cast<DevStatus*>(S->pin_rd);
     e = cudaMemcpyAsync(hst, S->status, sizeof(DevStatus), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return map_cuda_error(e);
+    prof_flush(S);
     if (hst->error) {
         if (debug_on()) debug_log("device status %d at %d detail %lld", hst->error, hst->where, hst->detail);
         return hst->error;
     }
-    S->stats.kernel_launches = launches;
+    S->stats.kernel_launches = S->launches;
     S->stats.alg_bytes = 12 * N;
     return QZGPU_NO_ERROR;
 }

@@ -50,6 +50,42 @@ void debug_after(cudaStream_t st, const char* what) {
     if (e != cudaSuccess) debug_log("%s: %s", what, cudaGetErrorString(e));
 }
 
+cudaEvent_t prof_begin(Storage* S, cudaStream_t st) {
+    if (!S->profile) return nullptr;
+    if (S->ev_next + 2 > S->ev_pool.size()) {
+        size_t grow = S->ev_pool.size() ? S->ev_pool.size() : 1024;
+        for (size_t i = 0; i < grow; ++i) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+            S->ev_pool.push_back(e);
+        }
+    }
+    cudaEvent_t a = S->ev_pool[S->ev_next++];
+    cudaEventRecord(a, st);
+    return a;
+}
+
+void prof_end(Storage* S, cudaStream_t st, const char* name, long long bytes, cudaEvent_t a) {
+    ++S->launches;
+    if (!a) return;
+    cudaEvent_t b = S->ev_pool[S->ev_next++];
+    cudaEventRecord(b, st);
+    S->prof_pending.push_back(Storage::ProfRec{name, a, b, bytes});
+}
+
+void prof_flush(Storage* S) {
+    for (auto& r : S->prof_pending) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, r.a, r.b) != cudaSuccess) continue;
+        auto& g = S->prof[r.name];
+        g.launches += 1;
+        g.ms += ms;
+        g.bytes += r.bytes;
+    }
+    S->prof_pending.clear();
+    S->ev_next = 0;
+}
+
 static const char* dump_dir() {
     static const char* d = getenv("QZGPU_DUMP");
     return (d && *d) ? d : nullptr;
@@ -92,7 +128,7 @@ struct Carver {
 };
 
 struct Caps {
-    size_t N, nb, init_tiles, hist, small, med, large, rulers, rtiles, aux;
+    size_t N, nb, init_tiles, hist, med, large, rulers, rtiles, aux;
 };
 
 Caps caps_for(long long cap_bytes, int cap_blocks) {
@@ -100,9 +136,9 @@ Caps caps_for(long long cap_bytes, int cap_blocks) {
     c.N = (size_t)cap_bytes;
     c.nb = (size_t)cap_blocks;
     c.init_tiles = c.N / kInitTile + c.nb + 1;
-    size_t fwd_tiles = 2 * (c.N / kRT) + 2;
+    // radix tiles: sum over groups longer than kMedMax of ceil(len / kRT)
+    size_t fwd_tiles = c.N / kRT + c.N / (kMedMax + 1) + 2;
     c.hist = 256 * std::max(fwd_tiles, c.init_tiles);
-    c.small = c.N / 2 + 1;
     c.med = c.N / (kSmallMax + 1) + 1;
     c.large = c.N / (kMedMax + 1) + 2;
     c.rulers = (c.N >> kMinStrideLog2) + c.nb + 1;
@@ -121,7 +157,6 @@ size_t layout(Storage* S, char* base, const Caps& c) {
     s->hist = cv.take<uint32_t>(c.hist);
     s->hist_cap = c.hist;
     s->partial = cv.take<uint32_t>(1024);
-    s->split_part = cv.take<int>(2 * kSplitGrid);
     s->counters = cv.take<int>(64);
     s->status = cv.take<DevStatus>(1);
     s->blk_off = cv.take<int>(c.nb + 1);
@@ -143,18 +178,23 @@ size_t layout(Storage* S, char* base, const Caps& c) {
     f.key = cv.take<uint32_t>(c.N);
     for (int i = 0; i < 2; ++i) {
         f.W[i] = cv.take<int>(c.N);
-        f.P[i] = cv.take<int>(c.N);
         f.G[i] = cv.take<int>(c.N);
         f.wsk[i] = cv.take<uint32_t>(c.N);
         f.wsv[i] = cv.take<int>(c.N);
     }
-    f.list[0] = cv.take<int2>(c.small);
-    f.list[1] = cv.take<int2>(c.med);
-    f.list[2] = cv.take<int2>(c.large);
+    f.list_med = cv.take<int2>(c.med);
+    f.list_large = cv.take<int2>(c.large);
     f.ltc = cv.take<uint32_t>(c.large + 1);
     f.llen = cv.take<uint32_t>(c.large + 1);
     f.ltbase = cv.take<uint32_t>(c.large + 1);
     f.lwbase = cv.take<uint32_t>(c.large + 1);
+    size_t wt = c.N / 256 + 2;
+    f.p_surv = cv.take<uint32_t>(wt);
+    f.p_sub = cv.take<int>(wt);
+    f.p_grp = cv.take<int>(wt);
+    f.c_surv = cv.take<uint32_t>(1024);
+    f.c_sub = cv.take<int>(1024);
+    f.c_grp = cv.take<int>(1024);
     size_t fwd_end = cv.off;
     // inverse layout, aliasing the forward buffers
     cv.off = shared_start;
@@ -295,6 +335,8 @@ int storage_init(Storage* S, long long cap_bytes, int cap_blocks) {
 }
 
 void storage_free(Storage* S) {
+    for (auto e : S->ev_pool) cudaEventDestroy(e);
+    S->ev_pool.clear();
     if (S->stream) cudaStreamDestroy(S->stream);
     if (S->dev) cudaFree(S->dev);
     if (S->pin) cudaFreeHost(S->pin);
@@ -546,6 +588,37 @@ int qzgpu_bwt_decode_device(qzgpu_storage* storage, int nblocks, const int* n, c
     cudaError_t e = cudaSetDevice(storage->device);
     if (e != cudaSuccess) return map_cuda_error(e);
     return inverse_run(storage, nblocks, n, indexes, d_U, d_T, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int qzgpu_storage_round_counts(const qzgpu_storage* storage, long long* active, int max) {
+    if (!storage || max < 0 || (max > 0 && !active)) return QZGPU_BAD_PARAMETER;
+    int n = (int)storage->rounds_active.size();
+    for (int i = 0; i < n && i < max; ++i) active[i] = storage->rounds_active[i];
+    return n;
+}
+
+int qzgpu_storage_profile(qzgpu_storage* storage, int enable) {
+    if (!storage) return QZGPU_BAD_PARAMETER;
+    std::lock_guard<std::mutex> lk(storage->mu);
+    storage->profile = enable != 0;
+    return QZGPU_NO_ERROR;
+}
+
+int qzgpu_storage_profile_read(qzgpu_storage* storage, qzgpu_kernel_time* out, int max, int reset) {
+    if (!storage || max < 0 || (max > 0 && !out)) return QZGPU_BAD_PARAMETER;
+    std::lock_guard<std::mutex> lk(storage->mu);
+    std::vector<std::pair<std::string, Storage::ProfAgg>> v(storage->prof.begin(), storage->prof.end());
+    std::sort(v.begin(), v.end(), [](const auto& x, const auto& y) { return x.second.ms > y.second.ms; });
+    for (int i = 0; i < max && i < (int)v.size(); ++i) {
+        memset(out[i].name, 0, sizeof(out[i].name));
+        strncpy(out[i].name, v[i].first.c_str(), sizeof(out[i].name) - 1);
+        out[i].launches = v[i].second.launches;
+        out[i].ms = v[i].second.ms;
+        out[i].alg_bytes = v[i].second.bytes;
+    }
+    int n = (int)v.size();
+    if (reset) storage->prof.clear();
+    return n;
 }
 
 int qzgpu_storage_last_stats(const qzgpu_storage* storage, qzgpu_stats* out) {

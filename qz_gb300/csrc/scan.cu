@@ -80,15 +80,16 @@ __global__ void __launch_bounds__(kThreads) k_scan_apply(const uint32_t* in,
     }
 }
 
-void scan_exclusive(const uint32_t* in, uint32_t* out, int len, const int* len_dev, uint32_t* partial,
-                    uint32_t* total_dev, cudaStream_t st, int* launches) {
-    k_scan_reduce<<<kScanGrid, kThreads, 0, st>>>(in, len, len_dev, partial);
-    QZ_DBG(st, "k_scan_reduce");
-    k_scan_top<<<1, kThreads, 0, st>>>(partial, kScanGrid, total_dev);
-    QZ_DBG(st, "k_scan_top");
-    k_scan_apply<<<kScanGrid, kThreads, 0, st>>>(in, out, len, len_dev, partial);
-    QZ_DBG(st, "k_scan_apply");
-    if (launches) *launches += 3;
+void scan_exclusive(Storage* S, const uint32_t* in, uint32_t* out, int len, const int* len_dev,
+                    uint32_t* total_dev, cudaStream_t st) {
+    uint32_t* partial = S->partial;
+    // bytes assume the host length; device-sized scans report 0
+    long long b = len_dev ? 0 : 12ll * len;
+    QZ_LAUNCH(S, st, "k_scan_reduce", b / 3,
+              k_scan_reduce<<<kScanGrid, kThreads, 0, st>>>(in, len, len_dev, partial));
+    QZ_LAUNCH(S, st, "k_scan_top", 8 * kScanGrid, k_scan_top<<<1, kThreads, 0, st>>>(partial, kScanGrid, total_dev));
+    QZ_LAUNCH(S, st, "k_scan_apply", 2 * b / 3,
+              k_scan_apply<<<kScanGrid, kThreads, 0, st>>>(in, out, len, len_dev, partial));
 }
 
 }  // namespace qz

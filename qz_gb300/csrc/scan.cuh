@@ -10,8 +10,9 @@ constexpr int kScanGrid = 256;              // CTAs in the reduce/apply phases
 constexpr int kScanItems = 4;               // uint32 per thread per tile (one uint4)
 constexpr int kScanTile = kThreads * kScanItems;
 
-// `len_dev` (if not null) overrides `len`.
-void scan_exclusive(const uint32_t* in, uint32_t* out, int len, const int* len_dev, uint32_t* partial,
-                    uint32_t* total_dev, cudaStream_t st, int* launches);
+struct Storage;
+// `len_dev` (if not null) overrides `len`.  Uses S->partial as scratch.
+void scan_exclusive(Storage* S, const uint32_t* in, uint32_t* out, int len, const int* len_dev,
+                    uint32_t* total_dev, cudaStream_t st);
 
 }  // namespace qz

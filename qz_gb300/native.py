@@ -42,6 +42,11 @@ class Stats(ctypes.Structure):
                 ("active_total", ctypes.c_longlong), ("alg_bytes", ctypes.c_longlong)]
 
 
+class KernelTime(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_int), ("ms", ctypes.c_double),
+                ("alg_bytes", ctypes.c_longlong)]
+
+
 _u8p = ctypes.POINTER(ctypes.c_uint8)
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _vp = ctypes.c_void_p
@@ -63,6 +68,9 @@ SIGNATURES = {
     "qzgpu_bwt_encode_device": (ctypes.c_int, [_vp, ctypes.c_int, _i32p, _vp, _vp, _i32p, _vp]),
     "qzgpu_bwt_decode_device": (ctypes.c_int, [_vp, ctypes.c_int, _i32p, _i32p, _vp, _vp, _vp]),
     "qzgpu_storage_last_stats": (ctypes.c_int, [_vp, ctypes.POINTER(Stats)]),
+    "qzgpu_storage_profile": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "qzgpu_storage_round_counts": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
+    "qzgpu_storage_profile_read": (ctypes.c_int, [_vp, ctypes.POINTER(KernelTime), ctypes.c_int, ctypes.c_int]),
 }
 
 
