@@ -43,6 +43,7 @@ extern "C" {
 #define QZGPU_GPU_NOT_SUPPORTED (-8)
 #define QZGPU_GPU_NOT_ENOUGH_MEMORY (-9)
 #define QZGPU_TIMEOUT (-10)
+#define QZGPU_BLOCK_TOO_LARGE (-11)
 
 /* libbsc feature bits (bsc.rs:32-36).  Accepted for signature compatibility;
  * the GPU path is always taken and never falls back to the CPU. */
@@ -153,6 +154,33 @@ int qzgpu_storage_profile(qzgpu_storage *storage, int enable);
 /* Copies up to `max` records (largest total time first); returns the number
  * of kernels recorded.  reset != 0 clears the records afterwards. */
 int qzgpu_storage_profile_read(qzgpu_storage *storage, qzgpu_kernel_time *out, int max, int reset);
+
+/* ------------------------------------------------------------------------- */
+/* Allocation-free inverse BWT.                                               */
+/* ------------------------------------------------------------------------- */
+
+/* Largest block qzgpu_bwt_decode_noalloc accepts (1 MiB). */
+#define QZGPU_NOALLOC_MAX_BLOCK (1 << 20)
+
+/* Inverse BWT of one block for callers that cannot allocate device memory
+ * while they run (a host runtime that hands out all device memory up front
+ * and forbids later cudaMalloc/cudaFree, or a thread that must not take the
+ * allocator's locks).  No counterpart in the reference: libbsc's
+ * bsc_bwt_decode allocates its own work arrays.
+ *
+ * d_U (input BWT) and d_T (output block) are device pointers of n bytes; they
+ * may be the same buffer.  Work runs on `stream` (a cudaStream_t, NULL for the
+ * legacy default stream) and the call returns when the result is final.  It
+ * calls no cudaMalloc, cudaFree or other allocating routine: its scratch is a
+ * fixed 6 MiB device array that every GPU loading this library holds until the
+ * process exits.  The first call on a device looks that array's address up
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls in the process share the array, so calls whose GPU work overlaps
+ * (other host threads, other streams) race and must be serialised by the
+ * caller.  Returns 0, QZGPU_BLOCK_TOO_LARGE for n > QZGPU_NOALLOC_MAX_BLOCK,
+ * QZGPU_DATA_CORRUPT for an index or BWT that cannot be inverted, or another
+ * negative code. */
+int qzgpu_bwt_decode_noalloc(const unsigned char *d_U, unsigned char *d_T, int n, int index, void *stream);
 
 #ifdef __cplusplus
 }

@@ -18,6 +18,7 @@
 // Every row is read twice; every wait is a bounded loop and a broken LF cycle
 // (corrupt input) is reported as QZGPU_DATA_CORRUPT.
 #include <algorithm>
+#include <mutex>
 
 #include "engine.h"
 #include "scan.cuh"
@@ -321,3 +322,144 @@ int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t*
 }
 
 }  // namespace qz
+
+// ------------------------------------------------------------------ allocation-free inverse
+//
+// For callers that cannot allocate device memory while they run: a pipeline
+// stage inside a host runtime that owns every device allocation up front
+// (and forbids cudaMalloc/cudaFree later), or code on a thread that must not
+// take the allocator's locks.  The caller passes device input and output;
+// all scratch of the inverse lives in one file-scope array below, sized for
+// blocks of up to QZGPU_NOALLOC_MAX_BLOCK bytes.
+
+namespace qz {
+namespace noalloc {
+
+constexpr long long kMaxN = QZGPU_NOALLOC_MAX_BLOCK;
+constexpr long long kMaxTiles = (kMaxN + kInitTile - 1) / kInitTile;
+constexpr int kStrideLog2 = 5;
+constexpr long long kMaxRulers = (kMaxN >> kStrideLog2) + 1;
+constexpr long long kMaxRTiles = (kMaxRulers + kThreads - 1) / kThreads;
+
+constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+// byte offsets inside the scratch array
+constexpr size_t kOffLF = 0;
+constexpr size_t kOffHist = align256(kOffLF + 4 * (kMaxN + 2));
+constexpr size_t kOffPartial = align256(kOffHist + 4 * 256 * kMaxTiles);
+constexpr size_t kOffRuler = align256(kOffPartial + 4 * 1024);
+constexpr size_t kRulerBytes = align256(4 * kMaxRulers);
+constexpr size_t kOffTiles = kOffRuler + 5 * kRulerBytes;
+constexpr size_t kOffRTiles = align256(kOffTiles + 8 * kMaxTiles);
+constexpr size_t kOffTables = align256(kOffRTiles + 8 * kMaxRTiles);  // off, idx, tbase, rbase
+constexpr size_t kOffStatus = align256(kOffTables + 4 * 16);
+constexpr size_t kBytes = align256(kOffStatus + sizeof(DevStatus));
+static_assert(kBytes <= (6u << 20), "allocation-free scratch exceeds its stated 6 MiB");
+
+}  // namespace noalloc
+
+// Every GPU that loads this library holds this array until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[noalloc::kBytes];
+
+// Per-block tables of a single-block inverse, built on the device.
+__global__ void k_noalloc_tables(char* scratch, int n, int index) {
+    using namespace noalloc;
+    int* tab = reinterpret_cast<int*>(scratch + kOffTables);
+    int m = (n + kInitTile - 1) / kInitTile;
+    int M = (n >> kStrideLog2) + 1;
+    if (threadIdx.x == 0) {
+        tab[0] = 0;  // off
+        tab[1] = n;
+        tab[2] = index;  // idx
+        tab[4] = 0;      // tbase
+        tab[5] = m;
+        tab[6] = 0;      // rbase
+        tab[7] = M;
+        *reinterpret_cast<DevStatus*>(scratch + kOffStatus) = DevStatus{0, 0, 0};
+    }
+    int2* tiles = reinterpret_cast<int2*>(scratch + kOffTiles);
+    for (int j = threadIdx.x; j < m; j += blockDim.x) tiles[j] = make_int2(0, j * kInitTile);
+    int2* rtiles = reinterpret_cast<int2*>(scratch + kOffRTiles);
+    int nrt = (M + kThreads - 1) / kThreads;
+    for (int j = threadIdx.x; j < nrt; j += blockDim.x) rtiles[j] = make_int2(0, j * kThreads);
+}
+
+namespace {
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[256];
+
+// Device address of the scratch array for the current device, looked up once
+// per device (host code must not use the array's name as a device address).
+int noalloc_scratch(char** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return map_cuda_error(e);
+    if (dev < 0 || dev >= 256) return QZGPU_GPU_NOT_SUPPORTED;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) return map_cuda_error(e == cudaSuccess ? cudaErrorInvalidSymbol : e);
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = static_cast<char*>(g_noalloc_ptr[dev]);
+    return QZGPU_NO_ERROR;
+}
+
+}  // namespace
+
+}  // namespace qz
+
+extern "C" int qzgpu_bwt_decode_noalloc(const unsigned char* d_U, unsigned char* d_T, int n, int index,
+                                        void* stream) {
+    using namespace qz;
+    using namespace qz::noalloc;
+    if (n < 0 || (n > 0 && (!d_U || !d_T))) return QZGPU_BAD_PARAMETER;
+    if (n > QZGPU_NOALLOC_MAX_BLOCK) return QZGPU_BLOCK_TOO_LARGE;
+    if (n == 0) return QZGPU_NO_ERROR;
+    if (index < 1 || index > n) return QZGPU_DATA_CORRUPT;
+    char* sc = nullptr;
+    int rc = noalloc_scratch(&sc);
+    if (rc) return rc;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    int* tab = reinterpret_cast<int*>(sc + kOffTables);
+    int m = (n + kInitTile - 1) / kInitTile;
+    int M = (n >> kStrideLog2) + 1;
+    int nrt = (M + kThreads - 1) / kThreads;
+    int* rul = reinterpret_cast<int*>(sc + kOffRuler);
+    int* rnext0 = rul;
+    int* rdist0 = reinterpret_cast<int*>(sc + kOffRuler + kRulerBytes);
+    int* rnext1 = reinterpret_cast<int*>(sc + kOffRuler + 2 * kRulerBytes);
+    int* rdist1 = reinterpret_cast<int*>(sc + kOffRuler + 3 * kRulerBytes);
+    int* rlen = reinterpret_cast<int*>(sc + kOffRuler + 4 * kRulerBytes);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(sc + kOffHist);
+    DevStatus* dst = reinterpret_cast<DevStatus*>(sc + kOffStatus);
+
+    // launch bookkeeping for the shared scan helper only; it owns no memory
+    Storage ctx;
+    ctx.partial = reinterpret_cast<uint32_t*>(sc + kOffPartial);
+
+    k_noalloc_tables<<<1, kThreads, 0, st>>>(sc, n, index);
+    InvArgs a{d_U, tab, tab + 2, tab + 4, tab + 6, reinterpret_cast<const int2*>(sc + kOffTiles),
+              reinterpret_cast<int*>(sc + kOffLF), kStrideLog2, dst};
+    k_inv_up<<<m, kThreads, 0, st>>>(a, hist);
+    scan_exclusive(&ctx, hist, hist, 256 * m, nullptr, nullptr, st);
+    k_inv_down<<<m, kThreads, 0, st>>>(a, hist);
+    RulerArgs r{reinterpret_cast<const int2*>(sc + kOffRTiles), rnext0, rdist0, rlen};
+    k_inv_walk1<<<nrt, kThreads, 0, st>>>(a, r);
+    int* nx[2] = {rnext0, rnext1};
+    int* ds[2] = {rdist0, rdist1};
+    int cur = 0;
+    int jgrid = (M + kThreads - 1) / kThreads;
+    for (long long span = 1; span < (long long)M + 1; span <<= 1) {
+        k_inv_jump<<<jgrid, kThreads, 0, st>>>(M, nx[cur], ds[cur], nx[cur ^ 1], ds[cur ^ 1]);
+        cur ^= 1;
+    }
+    k_inv_walk2<<<nrt, kThreads, 0, st>>>(a, r, nx[cur], ds[cur], hist, d_T);
+    cudaError_t e = cudaGetLastError();
+    DevStatus hst{0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hst, dst, sizeof(hst), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return map_cuda_error(e);
+    return hst.error;
+}

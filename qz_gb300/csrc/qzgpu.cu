@@ -462,6 +462,7 @@ const char* qzgpu_error_string(int code) {
         case QZGPU_GPU_NOT_SUPPORTED: return "no usable GPU";
         case QZGPU_GPU_NOT_ENOUGH_MEMORY: return "not enough GPU memory";
         case QZGPU_TIMEOUT: return "timed out";
+        case QZGPU_BLOCK_TOO_LARGE: return "block larger than this entry point accepts";
         default: return "unknown error";
     }
 }

@@ -22,6 +22,8 @@ QZGPU_GPU_ERROR = -7
 QZGPU_GPU_NOT_SUPPORTED = -8
 QZGPU_GPU_NOT_ENOUGH_MEMORY = -9
 QZGPU_TIMEOUT = -10
+QZGPU_BLOCK_TOO_LARGE = -11
+QZGPU_NOALLOC_MAX_BLOCK = 1 << 20
 
 LIB_PATH = _build.LIB
 _lock = threading.Lock()
@@ -69,6 +71,7 @@ SIGNATURES = {
     "qzgpu_bwt_decode_device": (ctypes.c_int, [_vp, ctypes.c_int, _i32p, _i32p, _vp, _vp, _vp]),
     "qzgpu_storage_last_stats": (ctypes.c_int, [_vp, ctypes.POINTER(Stats)]),
     "qzgpu_storage_profile": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "qzgpu_bwt_decode_noalloc": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
     "qzgpu_storage_round_counts": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
     "qzgpu_storage_profile_read": (ctypes.c_int, [_vp, ctypes.POINTER(KernelTime), ctypes.c_int, ctypes.c_int]),
 }

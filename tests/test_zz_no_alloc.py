@@ -1,0 +1,55 @@
+"""The allocation-free inverse BWT (qzgpu_bwt_decode_noalloc) against the
+existing inverse entry point, through the C ABI.
+
+This entry point serves callers that cannot allocate device memory while they
+run, for example a host runtime that hands out all device memory up front and
+forbids later cudaMalloc/cudaFree.  Its scratch is a fixed device array shared
+by every call, so two calls in a row must both give the existing entry point's
+output (bit-exact: byte work has no tolerance).  This file is named to be
+collected last.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from qz_gb300 import bwt, native, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _noalloc(lib, d_u, d_t, n, index, stream):
+    return lib.qzgpu_bwt_decode_noalloc(ctypes.c_void_p(d_u), ctypes.c_void_p(d_t), int(n), int(index),
+                                        ctypes.c_void_p(stream))
+
+
+def test_noalloc_decode_matches_existing_entry_point():
+    torch = pytest.importorskip("torch")
+    lib = native.load()
+    bwt.init()
+    stream = torch.cuda.current_stream().cuda_stream
+    blocks = [
+        synth.sample_reads(synth.uniform_genome(60_000, seed=61), 2000, seed=62),  # 300,000 bytes of DNA
+        synth.quality_stream(8000, seed=63)[: native.QZGPU_NOALLOC_MAX_BLOCK],    # the 1 MiB limit exactly
+    ]
+    for t in blocks:  # two calls in a row share the scratch array
+        u, idx = bwt.bwt_encode(t)
+        expected = bwt.bwt_decode(u, idx)  # existing entry point
+        d_u = torch.from_numpy(np.ascontiguousarray(u)).cuda()
+        d_t = torch.empty_like(d_u)
+        rc = _noalloc(lib, d_u.data_ptr(), d_t.data_ptr(), len(u), idx, stream)
+        assert rc == native.QZGPU_NO_ERROR, native.error_string(rc)
+        torch.cuda.synchronize()
+        assert np.array_equal(d_t.cpu().numpy(), expected)
+        assert np.array_equal(expected, t)
+
+
+def test_noalloc_rejects_blocks_over_the_limit():
+    torch = pytest.importorskip("torch")
+    lib = native.load()
+    bwt.init()
+    n = native.QZGPU_NOALLOC_MAX_BLOCK + 1
+    d = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    rc = _noalloc(lib, d.data_ptr(), d.data_ptr(), n, 1, torch.cuda.current_stream().cuda_stream)
+    assert rc == native.QZGPU_BLOCK_TOO_LARGE
+    assert "larger" in native.error_string(rc)
