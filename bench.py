@@ -297,6 +297,34 @@ def run_gpu(args, rank: int, world: int):
                 "alg_bytes_per_launch": int(per_launch_bytes),
                 "traffic": (tr.get("bytes_per_launch") if isinstance(tr, dict) else tr)}
 
+    # ---- plain one-block-per-call path on the same device-resident inputs
+    plain = None
+    if args.plain_blocks:
+        offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+
+        def plain_step():
+            for b, n in enumerate(sizes):
+                if n == 0:
+                    continue
+                o = int(offs[b])
+                ix = st.encode_device([n], d_T.data_ptr() + o, d_U.data_ptr() + o, sptr)
+                st.decode_device([n], ix, d_U.data_ptr() + o, d_R.data_ptr() + o, sptr)
+
+        plain_step()
+        torch.cuda.synchronize(dev)
+        if not torch.equal(d_R, d_T):
+            raise SystemExit("plain-path round trip mismatch")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            plain_step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        pms = e0.elapsed_time(e1)
+        plain = {"value": round(N * args.steps / (pms / 1e3) / 1e6, 3), "unit": "MB/s",
+                 "ms_per_step": round(pms / args.steps, 3),
+                 "path": "one qzgpu_bwt_encode_device + qzgpu_bwt_decode_device call per block"}
+
     # ---- end to end through the host-buffer C ABI (copies inside the timed region)
     e2e = None
     if not args.no_e2e:
@@ -347,6 +375,7 @@ def run_gpu(args, rank: int, world: int):
             "active_per_round": rounds_active,
             "gpu_launches": launches,
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "kernels": kernels[:12],
+            "plain_per_block": plain,
         }
         print(json.dumps(line), flush=True)
     st.close()
@@ -364,6 +393,8 @@ def main():
     ap.add_argument("--reads", type=int, default=2_500_000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-blocks", action="store_true",
+                    help="also time the plain path: one forward + inverse call per block")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -17,7 +17,7 @@ namespace qz {
 // Segment classes of the per-round sort (by group length).
 constexpr int kSmallMax = 16;    // one thread, register bitonic network
 constexpr int kMedMax = 512;     // one warp, register bitonic sort across lanes
-constexpr int kRT = 2048;        // tile of the segmented radix sort (larger groups)
+constexpr int kOT = 4096;        // one CTA sorts a group of up to kOT slots; longer: onesweep tiles
 constexpr int kInitTile = 4096;  // text positions per tile of the per-block passes
 constexpr int kMaxRounds = 40;   // prefix doubling needs <= 31 rounds for n < 2^31
 
@@ -31,6 +31,9 @@ enum Counter {
     CNT_LHIST = 5,   // histogram entries of the large-group radix sort (256 per tile)
     CNT_ACTIVE_ALT = 6,
     CNT_MED_ELEMS = 8,  // slots covered by each listed class
+    CNT_TILE = 10,
+    CNT_TILE_ELEMS = 11,
+    CNT_TICKET = 12,    // tile tickets of a look-back radix pass
     CNT_LARGE_ELEMS = 9,
     CNT_SLOTS = 16,
 };
@@ -43,8 +46,11 @@ struct FwdBuffers {
     int* G[2];   // compact slots: group rank (SA position of the group's first slot)
     uint32_t* wsk[2];
     int* wsv[2];
-    int2* list_med;
-    int2* list_large;
+    int2* list_med;    // groups of 17..512 slots
+    int2* list_tile;   // groups of 513..4096 slots
+    int2* list_large;  // groups of more than 4096 slots
+    uint32_t* h4;      // large groups: digit counts of all four passes
+    unsigned long long* status64;  // look-back status per (tile, digit)
     uint32_t* ltc;     // large: tiles per group -> tile base
     uint32_t* llen;    // large: length per group -> workspace base
     uint32_t* ltbase;
@@ -130,7 +136,9 @@ struct Storage {
     size_t ev_next = 0;
     std::vector<ProfRec> prof_pending;
     std::map<std::string, ProfAgg> prof;
-    std::vector<int> rounds_active;  // active suffixes per round of the last forward call
+    std::vector<long long> rounds_active;  // active suffixes per round of the last forward call
+    long long sub_batch_bytes = 16ll << 20;  // forward: blocks grouped up to this size
+    unsigned radix_epoch = 0;                // tags look-back status words of each pass
 };
 
 size_t storage_device_bytes(long long cap_bytes, int cap_blocks);

@@ -29,12 +29,11 @@
 // stable ranking, shared-memory staged scatter).  The secondary-key gather is
 // fused into the sorts.
 #include "engine.h"
+#include "radix.cuh"
 #include "scan.cuh"
 
 namespace qz {
 
-constexpr int kRItems = kRT / kThreads;  // elements per thread in a radix tile
-constexpr int kRWarpSpan = kRT / kWarps; // contiguous elements per warp in a radix tile
 
 // ------------------------------------------------------------------ per-block alphabet
 
@@ -196,33 +195,64 @@ __device__ __forceinline__ void sort_group_regs(int s, int len, uint32_t* key, i
     }
 }
 
-// Groups of 2..16 slots: the thread of a group's first slot finds the group
-// from the group-rank array G and sorts it in registers.  Longer groups are
-// left to the listed sorts.
+// Groups of 2..16 slots.  Each warp takes a window of 32 consecutive slots;
+// group bounds come from ballots over the group ranks G, and every lane of a
+// group that lies inside the window computes its own rank in the group by
+// counting smaller keys (ties broken by slot), then writes its key and suffix
+// to that position.  A group that straddles the window end is sorted by the
+// thread holding its first slot, in registers.
 __global__ void __launch_bounds__(kThreads) k_sort_small(const int* __restrict__ d_A, const int* __restrict__ G,
                                                          uint32_t* __restrict__ key, int* __restrict__ W) {
-    int A = *d_A;
-    for (int k = blockIdx.x * kThreads + threadIdx.x; k < A; k += gridDim.x * kThreads) {
-        int g = G[k];
-        if (k > 0 && G[k - 1] == g) continue;
-        int L = 1;
-        while (L <= kSmallMax && k + L < A && G[k + L] == g) ++L;
-        if (L > kSmallMax || L < 2) continue;
-        if (L == 2) {
-            uint32_t k0 = key[k], k1 = key[k + 1];
-            if (k1 < k0) {
-                int w0 = W[k], w1 = W[k + 1];
-                key[k] = k1;
-                key[k + 1] = k0;
-                W[k] = w1;
-                W[k + 1] = w0;
+    const int A = *d_A;
+    const int ln = (int)lane_id();
+    const int nwin = (A + 31) / 32;
+    const int nwarps = gridDim.x * kWarps;
+    for (int win = blockIdx.x * kWarps + (int)warp_id(); win < nwin; win += nwarps) {
+        const int base = win * 32;
+        const int k = base + ln;
+        const bool valid = k < A;
+        int g = valid ? G[k] : -1;
+        int gp = __shfl_up_sync(0xffffffffu, g, 1);
+        if (ln == 0) gp = (base > 0) ? G[base - 1] : -2;
+        int gn = __shfl_down_sync(0xffffffffu, g, 1);
+        if (ln == 31) gn = (k + 1 < A) ? G[k + 1] : -2;
+        const bool head = valid && gp != g;
+        const bool tail = valid && (k + 1 >= A || gn != g);
+        const unsigned H = __ballot_sync(0xffffffffu, head);
+        const unsigned T = __ballot_sync(0xffffffffu, tail);
+        uint32_t kv = valid ? key[k] : 0u;
+        int wv = valid ? W[k] : 0;
+        // group start: highest head at or below this lane; end: lowest tail at or above
+        const unsigned hb = H & (0xffffffffu >> (31 - ln));
+        const unsigned tb = T & (0xffffffffu << ln);
+        const int s = hb ? 31 - __clz(hb) : -1;
+        const int e = tb ? __ffs(tb) - 1 : 32;
+        const bool inside = valid && s >= 0 && e < 32;
+        const int L = inside ? e - s + 1 : 0;
+        const bool mine = inside && L >= 2 && L <= kSmallMax;
+        // every lane runs the same number of shuffles (the longest group in the window)
+        int maxL = mine ? L : 0;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) maxL = max(maxL, __shfl_xor_sync(0xffffffffu, maxL, d));
+        int rank = 0;
+        for (int j = 0; j < maxL; ++j) {
+            int src = (mine ? s : 0) + j;
+            uint32_t kj = __shfl_sync(0xffffffffu, kv, src & 31);
+            if (mine && j < L) rank += (kj < kv || (kj == kv && src < ln)) ? 1 : 0;
+        }
+        if (mine) {
+            key[base + s + rank] = kv;
+            W[base + s + rank] = wv;
+        }
+        // a group that starts in this window and ends after it
+        if (head && !(T & (0xffffffffu << ln))) {
+            int L2 = 32 - ln;
+            while (L2 <= kSmallMax && k + L2 < A && G[k + L2] == g) ++L2;
+            if (L2 >= 2 && L2 <= kSmallMax) {
+                if (L2 <= 4) sort_group_regs<4>(k, L2, key, W);
+                else if (L2 <= 8) sort_group_regs<8>(k, L2, key, W);
+                else sort_group_regs<16>(k, L2, key, W);
             }
-        } else if (L <= 4) {
-            sort_group_regs<4>(k, L, key, W);
-        } else if (L <= 8) {
-            sort_group_regs<8>(k, L, key, W);
-        } else {
-            sort_group_regs<16>(k, L, key, W);
         }
     }
 }
@@ -306,151 +336,6 @@ __global__ void __launch_bounds__(kThreads) k_gather(const int* __restrict__ d_A
     }
 }
 
-// ------------------------------------------------------------------ large groups: segmented LSD radix sort
-
-__global__ void __launch_bounds__(kThreads) k_large_prep(const int2* __restrict__ list,
-                                                         const int* __restrict__ d_count,
-                                                         uint32_t* __restrict__ tcount,
-                                                         uint32_t* __restrict__ lens) {
-    int cnt = *d_count;
-    for (int i = blockIdx.x * kThreads + threadIdx.x; i < cnt; i += gridDim.x * kThreads) {
-        int len = list[i].y;
-        tcount[i] = (uint32_t)((len + kRT - 1) / kRT);
-        lens[i] = (uint32_t)len;
-    }
-}
-
-// largest s in [0, n) with tbase[s] <= tau
-__device__ __forceinline__ int seg_of_tile(const uint32_t* __restrict__ tbase, int n, uint32_t tau) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (tbase[mid] <= tau) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
-
-struct LargeArgs {
-    const int2* list;
-    const int* nseg;
-    const uint32_t* tbase;
-    const uint32_t* wbase;
-    const int* ntiles;
-    int* hist_len;  // written: 256 * tiles
-};
-
-__global__ void __launch_bounds__(kThreads) k_large_up(LargeArgs a, const uint32_t* __restrict__ srck,
-                                                       int src_compact, int shift,
-                                                       uint32_t* __restrict__ hist) {
-    __shared__ uint32_t h[256];
-    __shared__ int s_seg;
-    int TT = *a.ntiles, nseg = *a.nseg;
-    if (blockIdx.x == 0 && threadIdx.x == 0) *a.hist_len = 256 * TT;
-    for (int tau = blockIdx.x; tau < TT; tau += gridDim.x) {
-        if (threadIdx.x == 0) s_seg = seg_of_tile(a.tbase, nseg, (uint32_t)tau);
-        h[threadIdx.x] = 0;
-        __syncthreads();
-        int s = s_seg;
-        int2 d = a.list[s];
-        int j = tau - (int)a.tbase[s];
-        int m = (d.y + kRT - 1) / kRT;
-        int base = (src_compact ? d.x : (int)a.wbase[s]) + j * kRT;
-        int cnt = min(kRT, d.y - j * kRT);
-        for (int q = 0; q < kRT; q += kThreads) {
-            int i = q + threadIdx.x;
-            unsigned dg = i < cnt ? (srck[base + i] >> shift) & 255u : 256u;
-            unsigned peers = __match_any_sync(0xffffffffu, dg);
-            if (dg < 256u && lane_id() == (unsigned)(__ffs(peers) - 1)) atomicAdd(&h[dg], __popc(peers));
-        }
-        __syncthreads();
-        hist[(size_t)256 * a.tbase[s] + (size_t)threadIdx.x * m + j] = h[threadIdx.x];
-        __syncthreads();
-    }
-}
-
-// One stable 8-bit digit pass over a tile: warp match-based ranks, scatter
-// staged in shared memory so that runs of one digit leave as coalesced writes.
-__global__ void __launch_bounds__(kThreads, 3) k_large_down(LargeArgs a, const uint32_t* __restrict__ hist,
-                                                            const uint32_t* __restrict__ srck,
-                                                            const int* __restrict__ srcv, int src_compact,
-                                                            uint32_t* __restrict__ dstk, int* __restrict__ dstv,
-                                                            int dst_compact, int shift) {
-    __shared__ uint32_t skey[kRT];
-    __shared__ int sval[kRT];
-    __shared__ uint32_t wcnt[kWarps][256];
-    __shared__ uint32_t dig_off[256];
-    __shared__ uint32_t gbase[256];
-    __shared__ uint32_t sh[kWarps + 1];
-    __shared__ int s_seg;
-    int TT = *a.ntiles, nseg = *a.nseg;
-    const unsigned w = warp_id(), ln = lane_id();
-    const unsigned lt_mask = (1u << ln) - 1u;
-    for (int tau = blockIdx.x; tau < TT; tau += gridDim.x) {
-        if (threadIdx.x == 0) s_seg = seg_of_tile(a.tbase, nseg, (uint32_t)tau);
-#pragma unroll
-        for (int q = 0; q < kWarps; ++q) wcnt[q][threadIdx.x] = 0;
-        __syncthreads();
-        int s = s_seg;
-        int2 d = a.list[s];
-        int j = tau - (int)a.tbase[s];
-        int m = (d.y + kRT - 1) / kRT;
-        int srcbase = (src_compact ? d.x : (int)a.wbase[s]) + j * kRT;
-        int cnt = min(kRT, d.y - j * kRT);
-        uint32_t rk[kRItems];
-#pragma unroll
-        for (int it = 0; it < kRItems; ++it) {
-            int i = (int)w * kRWarpSpan + it * 32 + (int)ln;
-            bool valid = i < cnt;
-            uint32_t kv = valid ? srck[srcbase + i] : 0u;
-            unsigned dg = valid ? (kv >> shift) & 255u : 256u;
-            unsigned peers = __match_any_sync(0xffffffffu, dg);
-            unsigned before = __popc(peers & lt_mask);
-            uint32_t prev = valid ? wcnt[w][dg] : 0u;
-            __syncwarp();
-            if (valid && before == 0) wcnt[w][dg] = prev + __popc(peers);
-            __syncwarp();
-            rk[it] = prev + before;
-        }
-        __syncthreads();
-        {
-            unsigned dg = threadIdx.x;
-            uint32_t run = 0;
-#pragma unroll
-            for (int q = 0; q < kWarps; ++q) {
-                uint32_t c = wcnt[q][dg];
-                wcnt[q][dg] = run;
-                run += c;
-            }
-            uint32_t tot;
-            uint32_t ex = block_excl_sum(run, sh, &tot);
-            dig_off[dg] = ex;
-            int dstbase = dst_compact ? d.x : (int)a.wbase[s];
-            gbase[dg] = hist[(size_t)256 * a.tbase[s] + (size_t)dg * m + j] - a.wbase[s] + (uint32_t)dstbase;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int it = 0; it < kRItems; ++it) {
-            int i = (int)w * kRWarpSpan + it * 32 + (int)ln;
-            if (i < cnt) {
-                uint32_t kv = srck[srcbase + i];
-                unsigned dg = (kv >> shift) & 255u;
-                uint32_t lp = dig_off[dg] + wcnt[w][dg] + rk[it];
-                skey[lp] = kv;
-                sval[lp] = srcv[srcbase + i];
-            }
-        }
-        __syncthreads();
-        for (int i = threadIdx.x; i < cnt; i += kThreads) {
-            uint32_t kv = skey[i];
-            unsigned dg = (kv >> shift) & 255u;
-            uint32_t dst = gbase[dg] + ((uint32_t)i - dig_off[dg]);
-            dstk[dst] = kv;
-            dstv[dst] = sval[i];
-        }
-        __syncthreads();
-    }
-}
-
 // ------------------------------------------------------------------ split into groups
 //
 // After a sort, slot k (compact, SA order) holds suffix W[k] of group G[k]
@@ -478,6 +363,7 @@ struct SplitArgs {
     int* Wn;
     int* Gn;
     int2* list_med;
+    int2* list_tile;
     int2* list_large;
     int* counters;
     uint32_t* p_surv;  // per warp tile; exclusive prefix after the partial scan
@@ -637,8 +523,10 @@ __global__ void __launch_bounds__(kThreads) k_pscan_top(SplitArgs a, uint32_t* _
     if (threadIdx.x == 0) {
         *a.A_next = (int)carry;
         a.counters[CNT_MED] = 0;
+        a.counters[CNT_TILE] = 0;
         a.counters[CNT_LARGE] = 0;
         a.counters[CNT_MED_ELEMS] = 0;
+        a.counters[CNT_TILE_ELEMS] = 0;
         a.counters[CNT_LARGE_ELEMS] = 0;
     }
 }
@@ -717,6 +605,9 @@ __global__ void __launch_bounds__(kThreads) k_split_apply(SplitArgs a) {
                             if (L <= kMedMax) {
                                 a.list_med[atomicAdd(&a.counters[CNT_MED], 1)] = dsc;
                                 atomicAdd(&a.counters[CNT_MED_ELEMS], L);
+                            } else if (L <= kOT) {
+                                a.list_tile[atomicAdd(&a.counters[CNT_TILE], 1)] = dsc;
+                                atomicAdd(&a.counters[CNT_TILE_ELEMS], L);
                             } else {
                                 a.list_large[atomicAdd(&a.counters[CNT_LARGE], 1)] = dsc;
                                 atomicAdd(&a.counters[CNT_LARGE_ELEMS], L);
@@ -778,54 +669,33 @@ void sort_groups(Storage* S, const int* hc, int A, const int* d_A, uint32_t* key
     int* cnt = S->counters;
     const int sms = S->sms;
     int nmd = hc[CNT_MED], nlg = hc[CNT_LARGE];
-    long long small_el = (long long)A - hc[CNT_MED_ELEMS] - hc[CNT_LARGE_ELEMS];
+    long long small_el = (long long)A - hc[CNT_MED_ELEMS] - hc[CNT_TILE_ELEMS] - hc[CNT_LARGE_ELEMS];
     // every slot: group rank read; small groups: key and suffix read and written
-    QZ_LAUNCH(S, st, "k_sort_small", 4ll * A + 16ll * small_el,
+    QZ_LAUNCH(S, st, "k_sort_small", 12ll * A + 8ll * small_el,
               k_sort_small<<<grid_for(A, kThreads, sms * 16), kThreads, 0, st>>>(d_A, G, key, W));
     if (nmd > 0)
         QZ_LAUNCH(S, st, "k_sort_medium", 16ll * hc[CNT_MED_ELEMS] + 8ll * nmd,
                   k_sort_medium<<<grid_for(nmd, kWarps, sms * 16), kThreads, 0, st>>>(f.list_med, cnt + CNT_MED,
                                                                                       key, W));
-    if (nlg > 0) {
-        long long le = hc[CNT_LARGE_ELEMS];
-        QZ_LAUNCH(S, st, "k_large_prep", 16ll * nlg,
-                  k_large_prep<<<grid_for(nlg, kThreads, sms * 4), kThreads, 0, st>>>(f.list_large, cnt + CNT_LARGE,
-                                                                                      f.ltc, f.llen));
-        scan_exclusive(S, f.ltc, f.ltbase, 0, cnt + CNT_LARGE, (uint32_t*)(cnt + CNT_LTILES), st);
-        scan_exclusive(S, f.llen, f.lwbase, 0, cnt + CNT_LARGE, nullptr, st);
-        LargeArgs la{f.list_large, cnt + CNT_LARGE, f.ltbase, f.lwbase, cnt + CNT_LTILES, cnt + CNT_LHIST};
-        int grid = sms * 6;
-        const uint32_t* sk[4] = {key, f.wsk[0], f.wsk[1], f.wsk[0]};
-        const int* sv[4] = {W, f.wsv[0], f.wsv[1], f.wsv[0]};
-        uint32_t* dk[4] = {f.wsk[0], f.wsk[1], f.wsk[0], key};
-        int* dv[4] = {f.wsv[0], f.wsv[1], f.wsv[0], W};
-        for (int pass = 0; pass < 4; ++pass) {
-            int shift = 8 * pass;
-            QZ_LAUNCH(S, st, "k_large_up", 4 * le,
-                      k_large_up<<<grid, kThreads, 0, st>>>(la, sk[pass], pass == 0, shift, S->hist));
-            // histogram entries = 256 * tiles (count on device)
-            scan_exclusive(S, S->hist, S->hist, 0, cnt + CNT_LHIST, nullptr, st);
-            QZ_LAUNCH(S, st, "k_large_down", 16 * le,
-                      k_large_down<<<grid, kThreads, 0, st>>>(la, S->hist, sk[pass], sv[pass], pass == 0, dk[pass],
-                                                              dv[pass], pass == 3, shift));
-        }
-    }
+    sort_tile_groups(S, f.list_tile, cnt + CNT_TILE, hc[CNT_TILE], hc[CNT_TILE_ELEMS], key, W, st);
+    sort_big_groups(S, f.list_large, cnt + CNT_LARGE, nlg, hc[CNT_LARGE_ELEMS], key, W, st);
 }
 
 }  // namespace
 
-int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d_U, int* idx,
-                const int* aux_rate, int* aux_out, cudaStream_t st) {
-    if (nb < 0 || nb > S->cap_blocks) return QZGPU_BAD_PARAMETER;
+namespace {
+
+void add_round(Storage* S, int r, long long a) {
+    if ((int)S->rounds_active.size() <= r) S->rounds_active.resize(r + 1, 0);
+    S->rounds_active[r] += a;
+}
+
+// One sub-batch: blocks laid out back to back from d_T, using the storage
+// arrays from position 0.  Accumulates round counts into S.
+int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d_U, int* idx,
+                 const int* aux_rate, int* aux_out, cudaStream_t st, int* rounds_out) {
     long long N = 0;
-    for (int b = 0; b < nb; ++b) {
-        if (n[b] < 0) return QZGPU_BAD_PARAMETER;
-        N += n[b];
-    }
-    if (N > S->cap_bytes) return QZGPU_BAD_PARAMETER;
-    S->stats = qzgpu_stats{};
-    S->rounds_active.clear();
-    S->launches = 0;
+    for (int b = 0; b < nb; ++b) N += n[b];
     for (int b = 0; b < nb; ++b) idx[b] = n[b] <= 1 ? n[b] : -1;
     if (N == 0) return QZGPU_NO_ERROR;
     FwdBuffers& f = S->f;
@@ -838,7 +708,7 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
     for (int b = 0; b < nb; ++b)
         for (int s = off[b]; s < off[b + 1]; s += kInitTile) tiles.push_back(make_int2(b, s));
     // initial groups = blocks; blocks of <= kSmallMax bytes need no list
-    std::vector<int2> l1, l2;
+    std::vector<int2> l1, lt, l2;
     int cnt0[CNT_SLOTS] = {0};
     for (int b = 0; b < nb; ++b) {
         if (n[b] <= kSmallMax) continue;
@@ -846,6 +716,9 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
         if (n[b] <= kMedMax) {
             l1.push_back(dsc);
             cnt0[CNT_MED_ELEMS] += n[b];
+        } else if (n[b] <= kOT) {
+            lt.push_back(dsc);
+            cnt0[CNT_TILE_ELEMS] += n[b];
         } else {
             l2.push_back(dsc);
             cnt0[CNT_LARGE_ELEMS] += n[b];
@@ -859,7 +732,7 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
             if (aux_rate[b] > 0 && n[b] > 0) aux_total += (n[b] - 1) / aux_rate[b];
         }
     }
-    size_t need = sizeof(int) * (nb + 1) + sizeof(int2) * (tiles.size() + l1.size() + l2.size()) +
+    size_t need = sizeof(int) * (nb + 1) + sizeof(int2) * (tiles.size() + l1.size() + lt.size() + l2.size()) +
                   sizeof(int) * CNT_SLOTS + sizeof(int) * 2 * nb + 64 * 8;
     if (need > S->pin_tab_bytes || aux_total > 64 * S->cap_blocks) return QZGPU_BAD_PARAMETER;
     char* p = S->pin_tab;
@@ -872,9 +745,11 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
     char* h_off = put(off.data(), sizeof(int) * off.size());
     char* h_tiles = put(tiles.data(), sizeof(int2) * tiles.size());
     char* h_l1 = put(l1.data(), sizeof(int2) * l1.size());
+    char* h_lt = put(lt.data(), sizeof(int2) * lt.size());
     char* h_l2 = put(l2.data(), sizeof(int2) * l2.size());
     cnt0[CNT_ACTIVE] = (int)N;
     cnt0[CNT_MED] = (int)l1.size();
+    cnt0[CNT_TILE] = (int)lt.size();
     cnt0[CNT_LARGE] = (int)l2.size();
     char* h_cnt = put(cnt0, sizeof(cnt0));
     char* h_ar = aux_rate ? put(aux_rate, sizeof(int) * nb) : nullptr;
@@ -886,6 +761,7 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
     h2d(S->blk_off, h_off, sizeof(int) * off.size());
     h2d(S->tiles, h_tiles, sizeof(int2) * tiles.size());
     h2d(f.list_med, h_l1, sizeof(int2) * l1.size());
+    h2d(f.list_tile, h_lt, sizeof(int2) * lt.size());
     h2d(f.list_large, h_l2, sizeof(int2) * l2.size());
     h2d(S->counters, h_cnt, sizeof(cnt0));
     if (aux_rate) {
@@ -934,6 +810,7 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
         a.Wn = f.W[cur ^ 1];
         a.Gn = f.G[cur ^ 1];
         a.list_med = f.list_med;
+        a.list_tile = f.list_tile;
         a.list_large = f.list_large;
         a.counters = S->counters;
         a.p_surv = f.p_surv;
@@ -967,7 +844,7 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
     };
     split(N, true);
     dump_split();
-    S->rounds_active.push_back((int)N);
+    add_round(S, 0, N);
 
     int* hcnt = S->pin_rd;
     int round = 0;
@@ -987,13 +864,13 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
         first_split = false;
         if (A == 0) break;
         if (debug_on())
-            debug_log("round %d: active %d medium %d/%d large %d/%d", round, A, hcnt[CNT_MED], hcnt[CNT_MED_ELEMS],
-                      hcnt[CNT_LARGE], hcnt[CNT_LARGE_ELEMS]);
+            debug_log("round %d: active %d medium %d/%d tile %d/%d large %d/%d", round, A, hcnt[CNT_MED],
+                      hcnt[CNT_MED_ELEMS], hcnt[CNT_TILE], hcnt[CNT_TILE_ELEMS], hcnt[CNT_LARGE], hcnt[CNT_LARGE_ELEMS]);
         if (round >= kMaxRounds) {
             if (debug_on()) debug_log("no convergence after %d rounds", round);
             return QZGPU_GPU_ERROR;
         }
-        S->rounds_active.push_back(A);
+        add_round(S, round + 1, A);
         ga.round = round;
         // reads the suffix, gathers one rank, writes the key
         QZ_LAUNCH(S, st, "k_gather", 12ll * A,
@@ -1036,9 +913,48 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
             idx[b] = hcnt[b];
         }
     }
+    *rounds_out = round;
+    return QZGPU_NO_ERROR;
+}
+
+}  // namespace
+
+// Batches are processed in sub-batches of at most kSubBatchBytes (a larger
+// block alone): the random rank gathers and scatters of a round then stay
+// within one sub-batch's rank array, which the 126 MB L2 largely holds.
+int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d_U, int* idx,
+                const int* aux_rate, int* aux_out, cudaStream_t st) {
+    if (nb < 0 || nb > S->cap_blocks) return QZGPU_BAD_PARAMETER;
+    long long N = 0;
+    for (int b = 0; b < nb; ++b) {
+        if (n[b] < 0) return QZGPU_BAD_PARAMETER;
+        N += n[b];
+    }
+    if (N > S->cap_bytes) return QZGPU_BAD_PARAMETER;
+    S->stats = qzgpu_stats{};
+    S->rounds_active.clear();
+    S->launches = 0;
+    int max_rounds = 0;
+    long long off = 0;
+    int aoff = 0;
+    for (int b0 = 0; b0 < nb;) {
+        int b1 = b0;
+        long long sub = 0;
+        while (b1 < nb && (b1 == b0 || sub + n[b1] <= S->sub_batch_bytes)) sub += n[b1++];
+        int rounds = 0;
+        int rc = forward_core(S, b1 - b0, n + b0, d_T + off, d_U + off, idx + b0, aux_rate ? aux_rate + b0 : nullptr,
+                              aux_out ? aux_out + aoff : nullptr, st, &rounds);
+        if (rc) return rc;
+        if (aux_rate)
+            for (int b = b0; b < b1; ++b)
+                if (aux_rate[b] > 0 && n[b] > 0) aoff += (n[b] - 1) / aux_rate[b];
+        if (rounds > max_rounds) max_rounds = rounds;
+        off += sub;
+        b0 = b1;
+    }
     long long active_sum = 0;
-    for (int a : S->rounds_active) active_sum += a;
-    S->stats.rounds = round;
+    for (long long a : S->rounds_active) active_sum += a;
+    S->stats.rounds = max_rounds;
     S->stats.kernel_launches = S->launches;
     S->stats.active_total = active_sum;
     S->stats.alg_bytes = 15 * N + 28 * active_sum;

@@ -128,7 +128,7 @@ struct Carver {
 };
 
 struct Caps {
-    size_t N, nb, init_tiles, hist, med, large, rulers, rtiles, aux;
+    size_t N, nb, init_tiles, hist, med, tile, large, big_tiles, rulers, rtiles, aux;
 };
 
 Caps caps_for(long long cap_bytes, int cap_blocks) {
@@ -136,11 +136,13 @@ Caps caps_for(long long cap_bytes, int cap_blocks) {
     c.N = (size_t)cap_bytes;
     c.nb = (size_t)cap_blocks;
     c.init_tiles = c.N / kInitTile + c.nb + 1;
-    // radix tiles: sum over groups longer than kMedMax of ceil(len / kRT)
-    size_t fwd_tiles = c.N / kRT + c.N / (kMedMax + 1) + 2;
+    // look-back tiles: sum over groups longer than kOT of ceil(len / kOT)
+    size_t fwd_tiles = 2 * (c.N / kOT) + 2;
     c.hist = 256 * std::max(fwd_tiles, c.init_tiles);
     c.med = c.N / (kSmallMax + 1) + 1;
-    c.large = c.N / (kMedMax + 1) + 2;
+    c.tile = c.N / (kMedMax + 1) + 2;
+    c.large = c.N / (kOT + 1) + 2;
+    c.big_tiles = 2 * (c.N / kOT) + 2;
     c.rulers = (c.N >> kMinStrideLog2) + c.nb + 1;
     c.rtiles = c.rulers / kThreads + c.nb + 1;
     c.aux = 64 * c.nb + 64;
@@ -183,7 +185,10 @@ size_t layout(Storage* S, char* base, const Caps& c) {
         f.wsv[i] = cv.take<int>(c.N);
     }
     f.list_med = cv.take<int2>(c.med);
+    f.list_tile = cv.take<int2>(c.tile);
     f.list_large = cv.take<int2>(c.large);
+    f.h4 = cv.take<uint32_t>(1024 * c.large);
+    f.status64 = cv.take<unsigned long long>(256 * c.big_tiles);
     f.ltc = cv.take<uint32_t>(c.large + 1);
     f.llen = cv.take<uint32_t>(c.large + 1);
     f.ltbase = cv.take<uint32_t>(c.large + 1);
@@ -302,6 +307,8 @@ int storage_init(Storage* S, long long cap_bytes, int cap_blocks) {
     Caps c = caps_for(cap_bytes, cap_blocks);
     S->cap_bytes = cap_bytes;
     S->cap_blocks = cap_blocks;
+    const char* sb = getenv("QZGPU_SUB_BATCH_MB");
+    if (sb && atof(sb) > 0) S->sub_batch_bytes = (long long)(atof(sb) * (1 << 20));
     S->device = g.device;
     S->sms = g.sms;
     size_t bytes = layout(nullptr, nullptr, c);

@@ -1,0 +1,354 @@
+// Segmented sorts of (32-bit key, 32-bit value) pairs in compact slot space
+// for groups longer than a warp can sort (sm_103a, integer only).
+//
+//   * groups of kTileMin..kOT slots: one CTA sorts the whole group in shared
+//     memory, four 8-bit LSD passes, reading and writing global memory once;
+//   * longer groups: one stable 8-bit LSD pass per launch over 4096-slot
+//     tiles ("onesweep"): per-group digit totals for all four passes come from
+//     one histogram kernel; each tile takes a ticket in order, publishes its
+//     digit counts, and looks back over the tiles before it in the same group
+//     for its exclusive prefix (decoupled look-back), then scatters through
+//     shared memory so that each digit's run leaves as coalesced writes.
+//
+// Look-back waits are bounded: a tile only waits on tiles that took earlier
+// tickets, which publish their counts before they wait themselves; a wait that
+// exceeds its iteration limit records QZGPU_TIMEOUT in the status word and the
+// tile returns.
+#include "engine.h"
+#include "radix.cuh"
+#include "scan.cuh"
+
+namespace qz {
+
+constexpr int kOItems = kOT / kThreads;   // 16 slots per thread
+constexpr int kOWarpSpan = kOT / kWarps;  // 512 contiguous slots per warp
+constexpr unsigned long long kFlagAgg = 1ull << 32;
+constexpr unsigned long long kFlagInc = 2ull << 32;
+constexpr unsigned kSpinLimit = 1u << 24;
+
+// ------------------------------------------------------------------ one-tile groups
+
+// One CTA per group of kTileMin..kOT slots: four stable 8-bit passes in
+// shared memory (warp match-based ranks; ping-pong key/value buffers).
+__global__ void __launch_bounds__(kThreads) k_tile_sort(const int2* __restrict__ list, const int* __restrict__ d_count,
+                                                        uint32_t* __restrict__ key, int* __restrict__ val) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t* k0 = reinterpret_cast<uint32_t*>(smem);
+    int* v0 = reinterpret_cast<int*>(k0 + kOT);
+    uint32_t* k1 = reinterpret_cast<uint32_t*>(v0 + kOT);
+    int* v1 = reinterpret_cast<int*>(k1 + kOT);
+    uint32_t(*wcnt)[256] = reinterpret_cast<uint32_t(*)[256]>(v1 + kOT);
+    __shared__ uint32_t dig_off[256];
+    __shared__ uint32_t sh[kWarps + 1];
+    const unsigned w = warp_id(), ln = lane_id();
+    const unsigned lt_mask = (1u << ln) - 1u;
+    int cnt = *d_count;
+    for (int g = blockIdx.x; g < cnt; g += gridDim.x) {
+        int2 d = list[g];
+        int s = d.x, len = d.y;
+        for (int i = threadIdx.x; i < len; i += kThreads) {
+            k0[i] = key[s + i];
+            v0[i] = val[s + i];
+        }
+        uint32_t* ks = k0;
+        int* vs = v0;
+        uint32_t* kd = k1;
+        int* vd = v1;
+        for (int pass = 0; pass < 4; ++pass) {
+            const int shift = 8 * pass;
+#pragma unroll
+            for (int q = 0; q < kWarps; ++q) wcnt[q][threadIdx.x] = 0;
+            __syncthreads();
+            uint32_t rk[kOItems];
+#pragma unroll
+            for (int it = 0; it < kOItems; ++it) {
+                int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
+                bool valid = i < len;
+                unsigned dg = valid ? (ks[i] >> shift) & 255u : 256u;
+                unsigned peers = __match_any_sync(0xffffffffu, dg);
+                unsigned before = __popc(peers & lt_mask);
+                uint32_t prev = valid ? wcnt[w][dg] : 0u;
+                __syncwarp();
+                if (valid && before == 0) wcnt[w][dg] = prev + __popc(peers);
+                __syncwarp();
+                rk[it] = prev + before;
+            }
+            __syncthreads();
+            {
+                unsigned dg = threadIdx.x;
+                uint32_t run = 0;
+#pragma unroll
+                for (int q = 0; q < kWarps; ++q) {
+                    uint32_t c = wcnt[q][dg];
+                    wcnt[q][dg] = run;
+                    run += c;
+                }
+                uint32_t tot;
+                dig_off[dg] = block_excl_sum(run, sh, &tot);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int it = 0; it < kOItems; ++it) {
+                int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
+                if (i < len) {
+                    uint32_t kv = ks[i];
+                    unsigned dg = (kv >> shift) & 255u;
+                    uint32_t p = dig_off[dg] + wcnt[w][dg] + rk[it];
+                    kd[p] = kv;
+                    vd[p] = vs[i];
+                }
+            }
+            __syncthreads();
+            uint32_t* tk = ks;
+            ks = kd;
+            kd = tk;
+            int* tv = vs;
+            vs = vd;
+            vd = tv;
+        }
+        for (int i = threadIdx.x; i < len; i += kThreads) {
+            key[s + i] = ks[i];
+            val[s + i] = vs[i];
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ multi-tile groups
+
+__global__ void __launch_bounds__(kThreads) k_big_prep(const int2* __restrict__ list, const int* __restrict__ d_count,
+                                                       uint32_t* __restrict__ tcount, uint32_t* __restrict__ lens) {
+    int cnt = *d_count;
+    for (int i = blockIdx.x * kThreads + threadIdx.x; i < cnt; i += gridDim.x * kThreads) {
+        int len = list[i].y;
+        tcount[i] = (uint32_t)((len + kOT - 1) / kOT);
+        lens[i] = (uint32_t)len;
+    }
+}
+
+// largest s in [0, n) with tbase[s] <= tau
+__device__ __forceinline__ int big_seg_of_tile(const uint32_t* __restrict__ tbase, int n, uint32_t tau) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (tbase[mid] <= tau) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Digit counts of all four passes per group (order-independent), by tile.
+__global__ void __launch_bounds__(kThreads) k_big_hist(BigArgs a, const uint32_t* __restrict__ key,
+                                                       uint32_t* __restrict__ h4) {
+    __shared__ uint32_t h[4][256];
+    __shared__ int s_seg;
+    int TT = *a.ntiles, nseg = *a.nseg;
+    for (int tau = blockIdx.x; tau < TT; tau += gridDim.x) {
+        if (threadIdx.x == 0) s_seg = big_seg_of_tile(a.tbase, nseg, (uint32_t)tau);
+#pragma unroll
+        for (int p = 0; p < 4; ++p) h[p][threadIdx.x] = 0;
+        __syncthreads();
+        int s = s_seg;
+        int2 d = a.list[s];
+        int j = tau - (int)a.tbase[s];
+        int base = d.x + j * kOT;
+        int cnt = min(kOT, d.y - j * kOT);
+        for (int i = threadIdx.x; i < cnt; i += kThreads) {
+            uint32_t kv = key[base + i];
+#pragma unroll
+            for (int p = 0; p < 4; ++p) atomicAdd(&h[p][(kv >> (8 * p)) & 255u], 1u);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+            uint32_t v = h[p][threadIdx.x];
+            if (v) atomicAdd(&h4[((size_t)s * 4 + p) * 256 + threadIdx.x], v);
+        }
+        __syncthreads();
+    }
+}
+
+// Per group and pass: exclusive prefix over the 256 digits (in place).
+__global__ void __launch_bounds__(kThreads) k_big_bases(const int* __restrict__ d_nseg, uint32_t* __restrict__ h4) {
+    __shared__ uint32_t sh[kWarps + 1];
+    int n = *d_nseg * 4;
+    for (int r = blockIdx.x; r < n; r += gridDim.x) {
+        uint32_t v = h4[(size_t)r * 256 + threadIdx.x];
+        uint32_t tot;
+        h4[(size_t)r * 256 + threadIdx.x] = block_excl_sum(v, sh, &tot);
+    }
+}
+
+// One stable 8-bit pass with decoupled look-back.
+__global__ void __launch_bounds__(kThreads) k_big_pass(BigArgs a, const uint32_t* __restrict__ h4, int pass,
+                                                       unsigned epoch, const uint32_t* __restrict__ srck,
+                                                       const int* __restrict__ srcv, int src_compact,
+                                                       uint32_t* __restrict__ dstk, int* __restrict__ dstv,
+                                                       int dst_compact, unsigned long long* status,
+                                                       unsigned* ticket, DevStatus* st) {
+    __shared__ uint32_t skey[kOT];
+    __shared__ int sval[kOT];
+    __shared__ uint32_t wcnt[kWarps][256];
+    __shared__ uint32_t dig_off[256];
+    __shared__ uint32_t gbase[256];
+    __shared__ uint32_t sh[kWarps + 1];
+    __shared__ int s_tau, s_seg;
+    const unsigned w = warp_id(), ln = lane_id();
+    const unsigned lt_mask = (1u << ln) - 1u;
+    const int shift = 8 * pass;
+    const unsigned long long ep = (unsigned long long)epoch << 34;
+    int TT = *a.ntiles, nseg = *a.nseg;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_tau = (int)atomicAdd(ticket, 1u);
+            s_seg = s_tau < TT ? big_seg_of_tile(a.tbase, nseg, (uint32_t)s_tau) : 0;
+        }
+#pragma unroll
+        for (int q = 0; q < kWarps; ++q) wcnt[q][threadIdx.x] = 0;
+        __syncthreads();
+        int tau = s_tau;
+        if (tau >= TT) return;
+        int s = s_seg;
+        int2 d = a.list[s];
+        int j = tau - (int)a.tbase[s];
+        int srcbase = (src_compact ? d.x : (int)a.wbase[s]) + j * kOT;
+        int dstseg = dst_compact ? d.x : (int)a.wbase[s];
+        int cnt = min(kOT, d.y - j * kOT);
+        uint32_t rk[kOItems];
+#pragma unroll
+        for (int it = 0; it < kOItems; ++it) {
+            int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
+            bool valid = i < cnt;
+            uint32_t kv = valid ? srck[srcbase + i] : 0u;
+            unsigned dg = valid ? (kv >> shift) & 255u : 256u;
+            unsigned peers = __match_any_sync(0xffffffffu, dg);
+            unsigned before = __popc(peers & lt_mask);
+            uint32_t prev = valid ? wcnt[w][dg] : 0u;
+            __syncwarp();
+            if (valid && before == 0) wcnt[w][dg] = prev + __popc(peers);
+            __syncwarp();
+            rk[it] = prev + before;
+        }
+        __syncthreads();
+        {
+            unsigned dg = threadIdx.x;
+            uint32_t run = 0;
+#pragma unroll
+            for (int q = 0; q < kWarps; ++q) {
+                uint32_t c = wcnt[q][dg];
+                wcnt[q][dg] = run;
+                run += c;
+            }
+            // publish this tile's count, then find the counts of the tiles
+            // before it in the same group
+            volatile unsigned long long* my = status + (size_t)tau * 256 + dg;
+            uint32_t excl = 0;
+            if (j == 0) {
+                *my = ep | kFlagInc | run;
+            } else {
+                *my = ep | kFlagAgg | run;
+                int p = tau - 1;
+                for (;;) {
+                    volatile unsigned long long* q = status + (size_t)p * 256 + dg;
+                    unsigned long long v = *q;
+                    unsigned spins = 0;
+                    while (((v >> 34) != epoch || (v & (3ull << 32)) == 0) && spins < kSpinLimit) {
+                        __nanosleep(32);
+                        v = *q;
+                        ++spins;
+                    }
+                    if (spins >= kSpinLimit) {
+                        report(st, QZGPU_TIMEOUT, 20, tau);
+                        break;
+                    }
+                    excl += (uint32_t)(v & 0xffffffffull);
+                    if (v & kFlagInc) break;
+                    --p;
+                }
+                *my = ep | kFlagInc | (excl + run);
+            }
+            uint32_t tot;
+            dig_off[dg] = block_excl_sum(run, sh, &tot);
+            gbase[dg] = (uint32_t)dstseg + h4[((size_t)s * 4 + pass) * 256 + dg] + excl;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int it = 0; it < kOItems; ++it) {
+            int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
+            if (i < cnt) {
+                uint32_t kv = srck[srcbase + i];
+                unsigned dg = (kv >> shift) & 255u;
+                uint32_t lp = dig_off[dg] + wcnt[w][dg] + rk[it];
+                skey[lp] = kv;
+                sval[lp] = srcv[srcbase + i];
+            }
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt; i += kThreads) {
+            uint32_t kv = skey[i];
+            unsigned dg = (kv >> shift) & 255u;
+            uint32_t dst = gbase[dg] + ((uint32_t)i - dig_off[dg]);
+            dstk[dst] = kv;
+            dstv[dst] = sval[i];
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ host side
+
+namespace {
+int grid_cap(long long work, int per_cta, int cap) {
+    long long g = (work + per_cta - 1) / per_cta;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (int)g;
+}
+}  // namespace
+
+size_t tile_sort_smem() { return (size_t)kOT * 16 + sizeof(uint32_t) * kWarps * 256; }
+
+void sort_tile_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
+                      uint32_t* key, int* val, cudaStream_t st) {
+    if (host_count <= 0) return;
+    cudaFuncSetAttribute(k_tile_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_sort_smem());
+    QZ_LAUNCH(S, st, "k_tile_sort", 16 * elems,
+              k_tile_sort<<<grid_cap(host_count, 1, S->sms * 3), kThreads, tile_sort_smem(), st>>>(list, d_count,
+                                                                                                  key, val));
+}
+
+void sort_big_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
+                     uint32_t* key, int* val, cudaStream_t st) {
+    if (host_count <= 0) return;
+    FwdBuffers& f = S->f;
+    int* cnt = S->counters;
+    const int sms = S->sms;
+    QZ_LAUNCH(S, st, "k_big_prep", 16ll * host_count,
+              k_big_prep<<<grid_cap(host_count, kThreads, sms * 4), kThreads, 0, st>>>(list, d_count, f.ltc, f.llen));
+    scan_exclusive(S, f.ltc, f.ltbase, 0, d_count, (uint32_t*)(cnt + CNT_LTILES), st);
+    scan_exclusive(S, f.llen, f.lwbase, 0, d_count, nullptr, st);
+    BigArgs a{list, d_count, f.ltbase, f.lwbase, cnt + CNT_LTILES};
+    uint32_t* h4 = f.h4;
+    cudaMemsetAsync(h4, 0, sizeof(uint32_t) * 1024 * (size_t)host_count, st);
+    int grid = sms * 4;
+    QZ_LAUNCH(S, st, "k_big_hist", 4 * elems, k_big_hist<<<grid, kThreads, 0, st>>>(a, key, h4));
+    QZ_LAUNCH(S, st, "k_big_bases", 4096ll * host_count,
+              k_big_bases<<<grid_cap(4ll * host_count, 1, sms * 8), kThreads, 0, st>>>(d_count, h4));
+    const uint32_t* sk[4] = {key, f.wsk[0], f.wsk[1], f.wsk[0]};
+    const int* sv[4] = {val, f.wsv[0], f.wsv[1], f.wsv[0]};
+    uint32_t* dk[4] = {f.wsk[0], f.wsk[1], f.wsk[0], key};
+    int* dv[4] = {f.wsv[0], f.wsv[1], f.wsv[0], val};
+    // persistent grid of resident CTAs (64 registers and 43 KB of shared
+    // memory per CTA fit four per SM); tiles are taken by ticket
+    int pgrid = sms * 4;
+    for (int pass = 0; pass < 4; ++pass) {
+        unsigned epoch = ++S->radix_epoch & 0x3fffffffu;
+        if (epoch == 0) epoch = ++S->radix_epoch & 0x3fffffffu;
+        unsigned* ticket = reinterpret_cast<unsigned*>(cnt + CNT_TICKET);
+        cudaMemsetAsync(ticket, 0, sizeof(unsigned), st);
+        QZ_LAUNCH(S, st, "k_big_pass", 16 * elems,
+                  k_big_pass<<<pgrid, kThreads, 0, st>>>(a, h4, pass, epoch, sk[pass], sv[pass], pass == 0, dk[pass],
+                                                         dv[pass], pass == 3, f.status64, ticket, S->status));
+    }
+}
+
+}  // namespace qz

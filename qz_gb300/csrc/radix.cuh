@@ -1,0 +1,23 @@
+// Segmented (key, value) sorts for groups longer than a warp sorts.
+#pragma once
+#include "engine.h"
+
+namespace qz {
+
+struct BigArgs {
+    const int2* list;        // (first slot, length) per group
+    const int* nseg;         // number of groups (device)
+    const uint32_t* tbase;   // first tile of each group
+    const uint32_t* wbase;   // first workspace slot of each group
+    const int* ntiles;       // total tiles (device)
+};
+
+// Groups of kMedMax+1 .. kOT slots (one CTA each, all passes in shared memory).
+void sort_tile_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
+                      uint32_t* key, int* val, cudaStream_t st);
+// Groups longer than kOT slots (one decoupled look-back pass per digit).
+void sort_big_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
+                     uint32_t* key, int* val, cudaStream_t st);
+size_t tile_sort_smem();
+
+}  // namespace qz
