@@ -383,13 +383,119 @@ def run_gpu(args, rank: int, world: int):
         dist.destroy_process_group()
 
 
+# --------------------------------------------------------------------------- serving
+
+
+def run_serve(args, rank: int, world: int):
+    """Poisson arrivals of block requests (70% forward, 30% inverse of blocks
+    produced beforehand), sizes log-uniform 64 KiB-25 MiB, mixed DNA / quality /
+    header content; served by qzgpu_server_* with continuous batching."""
+    import torch
+
+    from qz_gb300 import bwt, synth
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    bwt.init()
+    reqs = synth.serving_requests(args.requests, rate_per_s=1.0, seed=6)
+    # inverse requests carry previously produced BWTs (made before timing)
+    inv_in = {}
+    inv_ids = [i for i, r in enumerate(reqs) if r[1] == "inv"]
+    with bwt.Storage(256 << 20, 256) as st:
+        chunk, used = [], 0
+        for i in inv_ids + [None]:
+            if i is None or used + len(reqs[i][3]) > (256 << 20):
+                if chunk:
+                    us, ix = st.encode_batch([reqs[j][3] for j in chunk])
+                    for j, u, p in zip(chunk, us, ix):
+                        inv_in[j] = (u, p)
+                chunk, used = [], 0
+            if i is not None:
+                chunk.append(i)
+                used += len(reqs[i][3])
+    total_bytes = sum(len(r[3]) for r in reqs)
+    mean_bytes = total_bytes / len(reqs)
+    srv = bwt.Server(hbm_budget=0, max_slots=args.slots, slot_bytes=64 << 20, slot_blocks=256)
+
+    def submit(i):
+        _, op, _, block = reqs[i]
+        if op == "inv":
+            u, p = inv_in[i]
+            return srv.submit_inverse(u, p)
+        return srv.submit_forward(block)
+
+    def run_point(gaps):
+        # gaps: seconds between arrivals (None = all at once)
+        tickets = [None] * len(reqs)
+        lat = []
+        done = threading.Event()
+
+        def waiter():
+            for i in range(len(reqs)):
+                while tickets[i] is None:
+                    time.sleep(0.0002)
+                r = srv.wait(tickets[i])
+                lat.append(r["latency_ms"])
+            done.set()
+
+        th = threading.Thread(target=waiter, daemon=True)
+        th.start()
+        t0 = time.perf_counter()
+        nxt = t0
+        for i in range(len(reqs)):
+            if gaps is not None:
+                nxt += gaps[i]
+                d = nxt - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+            tickets[i] = submit(i)
+        done.wait()
+        t1 = time.perf_counter()
+        lat.sort()
+        return {"mb_s": round(total_bytes / (t1 - t0) / 1e6, 3),
+                "p50_ms": round(lat[len(lat) // 2], 3), "p99_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),
+                "wall_s": round(t1 - t0, 3)}
+
+    for _ in range(max(1, args.warmup)):
+        run_point(None)
+    sat = run_point(None)
+    sat_rate = sat["mb_s"] * 1e6 / mean_bytes  # requests per second at saturation
+    rng = np.random.default_rng(60)
+    unit_gaps = rng.exponential(1.0, len(reqs))
+    points = []
+    for frac in (0.25, 0.5, 0.75, 1.0, 1.25, 1.5):
+        gaps = unit_gaps / (frac * sat_rate)
+        pt = run_point(gaps)
+        pt["offered_load"] = frac
+        pt["offered_mb_s"] = round(frac * sat["mb_s"], 3)
+        points.append(pt)
+    stats = srv.stats()
+    srv.close()
+    if rank == 0:
+        at1 = [p for p in points if p["offered_load"] == 1.0][0]
+        line = {
+            "metric": METRIC, "value": sat["mb_s"], "unit": "MB/s", "n_gpus": world, "steps": len(points),
+            "warmup": max(1, args.warmup), "ms_per_step": round(1e3 * sat["wall_s"], 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded reads of the workload's shape; no public dataset)",
+            "config": {"workload": f"serving: {len(reqs)} requests, Poisson arrivals, 70% forward / 30% inverse, "
+                                   "sizes log-uniform 64 KiB-25 MiB, 50% DNA / 30% quality / 20% header",
+                       "bytes_per_point": total_bytes, "slots": stats["slots"]},
+            "saturation": sat, "p50_ms_at_saturation_load": at1["p50_ms"], "p99_ms_at_saturation_load": at1["p99_ms"],
+            "load_points": points, "server": stats,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="chunk", choices=["chunk", "plain", "uneven", "repeat"])
+    ap.add_argument("--config", default="chunk", choices=["chunk", "plain", "uneven", "repeat", "serve"])
+    ap.add_argument("--requests", type=int, default=300, help="serve: requests per load point")
+    ap.add_argument("--slots", type=int, default=4, help="serve: device slots (bounded by free HBM)")
     ap.add_argument("--reads", type=int, default=2_500_000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -402,6 +508,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         run_reference(args, rank)
+    elif args.config == "serve":
+        run_serve(args, rank, world)
     else:
         run_gpu(args, rank, world)
 

@@ -156,6 +156,46 @@ int qzgpu_storage_profile(qzgpu_storage *storage, int enable);
 int qzgpu_storage_profile_read(qzgpu_storage *storage, qzgpu_kernel_time *out, int max, int reset);
 
 /* ------------------------------------------------------------------------- */
+/* Serving: concurrent block requests, continuous batching on resident slots. */
+/* ------------------------------------------------------------------------- */
+
+/* Replaces per-block bsc_compress / bsc_decompress calls issued concurrently
+ * by qz's rayon workers, chunk threads and decoder threads
+ * (compress_impl.rs:364-387, decompress_impl.rs:666-689, bsc.rs:285-288):
+ * requests from any host thread are batched onto device-resident slots. */
+#define QZGPU_OP_FORWARD 0
+#define QZGPU_OP_INVERSE 1
+
+typedef struct qzgpu_server qzgpu_server;
+
+/* Creates a server with as many slots (device storages of slot_bytes block
+ * bytes and slot_blocks blocks each; 0 picks 64 MiB / 256) as fit in
+ * hbm_budget_bytes (0: 80% of free HBM), at most max_slots (0: 4).  Each slot
+ * has a worker thread and a stream; a free worker batches every waiting
+ * request of one direction that fits its slot, in arrival order. */
+int qzgpu_server_create(qzgpu_server **server, long long hbm_budget_bytes, int max_slots, long long slot_bytes,
+                        int slot_blocks);
+/* Number of slots the server admitted within its budget. */
+int qzgpu_server_slots(const qzgpu_server *server);
+/* Queues one block: op QZGPU_OP_FORWARD (in = block, out receives U) or
+ * QZGPU_OP_INVERSE (in = U, index = primary index, out receives the block).
+ * in/out stay owned by the caller until the request is waited for.  Returns a
+ * ticket (>= 0) or a negative error. */
+long long qzgpu_server_submit(qzgpu_server *server, int op, const unsigned char *in, unsigned char *out, int n,
+                              int index);
+/* Waits up to timeout_ms (< 0: forever) for a ticket.  Returns 1 when done
+ * (status = the request's result code, index_out = primary index of a forward
+ * request, latency_ms = submit to completion, queue_ms = submit to start of its
+ * batch; the ticket is then released), 0 on timeout, or a negative error. */
+int qzgpu_server_wait(qzgpu_server *server, long long ticket, int timeout_ms, int *status, int *index_out,
+                      double *latency_ms, double *queue_ms);
+/* Counters: completed requests, batches, largest batch, most slots busy at
+ * once, requests waiting, slots.  Returns the number of counters. */
+int qzgpu_server_stats(const qzgpu_server *server, long long *out, int max);
+/* Finishes every queued request, then frees the slots. */
+int qzgpu_server_destroy(qzgpu_server *server);
+
+/* ------------------------------------------------------------------------- */
 /* Allocation-free inverse BWT.                                               */
 /* ------------------------------------------------------------------------- */
 

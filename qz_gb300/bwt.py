@@ -169,3 +169,80 @@ class Storage:
                                                 idx.ctypes.data_as(_i32p), ctypes.c_void_p(d_U),
                                                 ctypes.c_void_p(d_T), ctypes.c_void_p(stream)),
               "qzgpu_bwt_decode_device")
+
+
+class Server:
+    """Serving form over the C ABI: requests from any thread are batched
+    continuously onto device-resident slots (qzgpu_server_*)."""
+
+    FORWARD = 0
+    INVERSE = 1
+
+    def __init__(self, hbm_budget: int = 0, max_slots: int = 4, slot_bytes: int = 0, slot_blocks: int = 0):
+        import threading
+
+        self._lib = native.load()
+        h = ctypes.c_void_p()
+        check(self._lib.qzgpu_server_create(ctypes.byref(h), int(hbm_budget), int(max_slots), int(slot_bytes),
+                                            int(slot_blocks)), "qzgpu_server_create")
+        self._h = h
+        self._bufs = {}
+        self._lock = threading.Lock()
+        self.slots = self._lib.qzgpu_server_slots(h)
+
+    def _submit(self, op: int, data, index: int) -> int:
+        src = _as_u8(data)
+        n = len(src)
+        if n == 0:
+            src = np.zeros(1, np.uint8)
+        out = np.empty(max(n, 1), np.uint8)
+        t = self._lib.qzgpu_server_submit(self._h, op, src.ctypes.data_as(ctypes.c_void_p),
+                                          out.ctypes.data_as(ctypes.c_void_p), n, int(index))
+        check(t, "qzgpu_server_submit")
+        with self._lock:
+            self._bufs[t] = (src, out, n)
+        return t
+
+    def submit_forward(self, block) -> int:
+        return self._submit(self.FORWARD, block, 0)
+
+    def submit_inverse(self, u, index: int) -> int:
+        return self._submit(self.INVERSE, u, index)
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        st = ctypes.c_int32(0)
+        ix = ctypes.c_int32(0)
+        lat = ctypes.c_double(0)
+        q = ctypes.c_double(0)
+        rc = self._lib.qzgpu_server_wait(self._h, int(ticket), int(timeout_ms), ctypes.byref(st), ctypes.byref(ix),
+                                         ctypes.byref(lat), ctypes.byref(q))
+        check(rc, "qzgpu_server_wait")
+        if rc == 0:
+            return None
+        with self._lock:
+            src, out, n = self._bufs.pop(ticket)
+        check(st.value, "served request")
+        return {"out": out[:n], "index": ix.value, "latency_ms": lat.value, "queue_ms": q.value}
+
+    def stats(self) -> dict:
+        buf = (ctypes.c_longlong * 6)()
+        check(self._lib.qzgpu_server_stats(self._h, buf, 6), "qzgpu_server_stats")
+        keys = ("completed", "batches", "max_batch", "max_slots_busy", "waiting", "slots")
+        return dict(zip(keys, (int(v) for v in buf)))
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.qzgpu_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -110,8 +110,6 @@ struct Storage {
     // pinned host staging
     char* pin = nullptr;
     size_t pin_bytes = 0;
-    uint8_t* pin_T = nullptr;  // host-buffer calls: input staging
-    uint8_t* pin_U = nullptr;  // host-buffer calls: output staging
     char* pin_tab = nullptr;   // tables
     int* pin_rd = nullptr;     // small device->host readbacks
     size_t pin_tab_bytes = 0;
@@ -137,7 +135,7 @@ struct Storage {
     std::vector<ProfRec> prof_pending;
     std::map<std::string, ProfAgg> prof;
     std::vector<long long> rounds_active;  // active suffixes per round of the last forward call
-    long long sub_batch_bytes = 16ll << 20;  // forward: blocks grouped up to this size
+    long long sub_batch_bytes = 64ll << 20;  // forward: blocks grouped up to this size
     unsigned radix_epoch = 0;                // tags look-back status words of each pass
 };
 
@@ -157,6 +155,14 @@ int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t*
                 cudaStream_t st);
 
 int map_cuda_error(cudaError_t e);
+
+// Host-buffer batch calls on a storage the caller holds (copies in, runs,
+// copies out, synchronises the storage's stream).
+int check_blocks(int nblocks, const int* n, long long* total);
+int encode_host(Storage* S, int nb, const unsigned char* const* T, unsigned char* const* U, const int* n, int* idx,
+                const int* aux_rate, int* aux_out);
+int decode_host(Storage* S, int nb, const unsigned char* const* U, unsigned char* const* T, const int* n,
+                const int* idx);
 
 // Debug mode (environment QZGPU_DEBUG=1): every launch is followed by a
 // stream synchronize and an error check, and failures are logged to stderr.

@@ -321,7 +321,7 @@ int storage_init(Storage* S, long long cap_bytes, int cap_blocks) {
     layout(S, S->dev, c);
     S->pin_tab_bytes = pinned_table_bytes(c);
     size_t rd = sizeof(int) * (c.nb + 256);
-    S->pin_bytes = 2 * (c.N + 64) + S->pin_tab_bytes + rd + 64;
+    S->pin_bytes = S->pin_tab_bytes + rd + 64;
     e = cudaMallocHost(&S->pin, S->pin_bytes);
     if (e != cudaSuccess) {
         cudaFree(S->dev);
@@ -329,9 +329,7 @@ int storage_init(Storage* S, long long cap_bytes, int cap_blocks) {
         S->pin = nullptr;
         return QZGPU_NOT_ENOUGH_MEMORY;
     }
-    S->pin_T = reinterpret_cast<uint8_t*>(S->pin);
-    S->pin_U = S->pin_T + c.N + 64;
-    S->pin_tab = reinterpret_cast<char*>(S->pin_U + c.N + 64);
+    S->pin_tab = S->pin;
     S->pin_rd = reinterpret_cast<int*>(S->pin_tab + S->pin_tab_bytes);
     e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -358,7 +356,7 @@ using namespace qz;
 
 struct qzgpu_storage : public qz::Storage {};
 
-namespace {
+namespace qz {
 
 int check_blocks(int nblocks, const int* n, long long* total) {
     if (nblocks < 0 || (nblocks > 0 && !n)) return QZGPU_BAD_PARAMETER;
@@ -423,6 +421,10 @@ int decode_host(Storage* S, int nb, const unsigned char* const* U, unsigned char
     e = cudaStreamSynchronize(S->stream);
     return map_cuda_error(e);
 }
+
+}  // namespace qz
+
+namespace {
 
 // Runs fn on a pooled storage that fits `need` bytes (or a temporary one).
 template <typename Fn>

@@ -72,6 +72,14 @@ SIGNATURES = {
     "qzgpu_storage_last_stats": (ctypes.c_int, [_vp, ctypes.POINTER(Stats)]),
     "qzgpu_storage_profile": (ctypes.c_int, [_vp, ctypes.c_int]),
     "qzgpu_bwt_decode_noalloc": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
+    "qzgpu_server_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_longlong, ctypes.c_int, ctypes.c_longlong,
+                                           ctypes.c_int]),
+    "qzgpu_server_slots": (ctypes.c_int, [_vp]),
+    "qzgpu_server_submit": (ctypes.c_longlong, [_vp, ctypes.c_int, _vp, _vp, ctypes.c_int, ctypes.c_int]),
+    "qzgpu_server_wait": (ctypes.c_int, [_vp, ctypes.c_longlong, ctypes.c_int, _i32p, _i32p,
+                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "qzgpu_server_stats": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
+    "qzgpu_server_destroy": (ctypes.c_int, [_vp]),
     "qzgpu_storage_round_counts": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
     "qzgpu_storage_profile_read": (ctypes.c_int, [_vp, ctypes.POINTER(KernelTime), ctypes.c_int, ctypes.c_int]),
 }
