@@ -4,8 +4,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <condition_variable>
 #include <cstring>
+#include <functional>
 #include <map>
+#include <memory>
+#include <thread>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -138,6 +142,40 @@ struct Storage {
     long long sub_batch_bytes = 64ll << 20;  // forward: blocks grouped up to this size
     unsigned radix_epoch = 0;                // tags look-back status words of each pass
 };
+
+// Lane size of a multi-lane engine (block bytes one lane's sub-batch holds).
+constexpr long long kLaneBytes = 64ll << 20;
+
+// What callers hold as a qzgpu_storage: K lanes (scratch sets, each with its
+// stream and worker thread) that take sub-batches of a call concurrently.
+struct Engine {
+    long long cap_bytes = 0;
+    int cap_blocks = 0;
+    long long lane_bytes = 0;
+    int device = 0;
+    std::vector<std::unique_ptr<Storage>> lanes;
+    std::vector<std::thread> threads;
+    std::mutex mu;  // one call at a time
+    std::mutex jmu;
+    std::condition_variable jcv, dcv;
+    std::function<void(int)> job;
+    int job_gen = 0, job_done = 0;
+    bool stop = false;
+    bool profile = false;
+    qzgpu_stats stats{};
+    std::vector<long long> rounds_active;
+    std::map<std::string, Storage::ProfAgg> prof;
+};
+
+size_t engine_device_bytes(long long cap_bytes, int cap_blocks);
+int engine_init(Engine* E, long long cap_bytes, int cap_blocks);
+void engine_free(Engine* E);
+// forward (true) or inverse of nb blocks: host buffers (hin/hout) or device
+// buffers (d_in/d_out laid out back to back).  idx: per-block primary
+// indexes (written by a forward call, read by an inverse call).
+int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned char* const* hin,
+               unsigned char* const* hout, const unsigned char* d_in, unsigned char* d_out, int* idx,
+               cudaStream_t user_stream);
 
 size_t storage_device_bytes(long long cap_bytes, int cap_blocks);
 int storage_init(Storage* S, long long cap_bytes, int cap_blocks);

@@ -220,8 +220,6 @@ __global__ void __launch_bounds__(kThreads) k_sort_small(const int* __restrict__
         const bool tail = valid && (k + 1 >= A || gn != g);
         const unsigned H = __ballot_sync(0xffffffffu, head);
         const unsigned T = __ballot_sync(0xffffffffu, tail);
-        uint32_t kv = valid ? key[k] : 0u;
-        int wv = valid ? W[k] : 0;
         // group start: highest head at or below this lane; end: lowest tail at or above
         const unsigned hb = H & (0xffffffffu >> (31 - ln));
         const unsigned tb = T & (0xffffffffu << ln);
@@ -230,6 +228,9 @@ __global__ void __launch_bounds__(kThreads) k_sort_small(const int* __restrict__
         const bool inside = valid && s >= 0 && e < 32;
         const int L = inside ? e - s + 1 : 0;
         const bool mine = inside && L >= 2 && L <= kSmallMax;
+        // only lanes of groups sorted here read their key and suffix
+        uint32_t kv = mine ? key[k] : 0u;
+        int wv = mine ? W[k] : 0;
         // every lane runs the same number of shuffles (the longest group in the window)
         int maxL = mine ? L : 0;
 #pragma unroll
@@ -253,6 +254,99 @@ __global__ void __launch_bounds__(kThreads) k_sort_small(const int* __restrict__
                 else if (L2 <= 8) sort_group_regs<8>(k, L2, key, W);
                 else sort_group_regs<16>(k, L2, key, W);
             }
+        }
+    }
+}
+
+// Doubling rounds: secondary keys of all active slots, with groups of 2..16
+// slots that lie inside a 32-slot warp window sorted on the spot.  Each lane
+// gathers the key of its slot; group bounds come from ballots over G; a lane
+// of an in-window small group takes its rank in the group by counting smaller
+// keys (ties by slot) and writes key and suffix there.  Every other slot keeps
+// its suffix and gets its key written in place (sorted later by its class).
+__global__ void __launch_bounds__(kThreads) k_gather_small(const int* __restrict__ d_A, const int* __restrict__ G,
+                                                           uint32_t* __restrict__ key, int* __restrict__ W,
+                                                           GatherArgs ga) {
+    const int A = *d_A;
+    const int ln = (int)lane_id();
+    const int nwin = (A + 31) / 32;
+    const int nwarps = gridDim.x * kWarps;
+    for (int win = blockIdx.x * kWarps + (int)warp_id(); win < nwin; win += nwarps) {
+        const int base = win * 32;
+        const int k = base + ln;
+        const bool valid = k < A;
+        int g = valid ? G[k] : -1;
+        int x = valid ? W[k] : 0;
+        int gp = __shfl_up_sync(0xffffffffu, g, 1);
+        if (ln == 0) gp = (base > 0) ? G[base - 1] : -2;
+        int gn = __shfl_down_sync(0xffffffffu, g, 1);
+        if (ln == 31) gn = (k + 1 < A) ? G[k + 1] : -2;
+        uint32_t kv = 0;
+        if (valid) kv = rank_key(ga, block_span(ga, x), x);
+        const unsigned H = __ballot_sync(0xffffffffu, valid && gp != g);
+        const unsigned T = __ballot_sync(0xffffffffu, valid && (k + 1 >= A || gn != g));
+        const unsigned hb = H & (0xffffffffu >> (31 - ln));
+        const unsigned tb = T & (0xffffffffu << ln);
+        const int s = hb ? 31 - __clz(hb) : -1;
+        const int e = tb ? __ffs(tb) - 1 : 32;
+        const bool inside = valid && s >= 0 && e < 32;
+        const int L = inside ? e - s + 1 : 0;
+        const bool mine = inside && L >= 2 && L <= kSmallMax;
+        int maxL = mine ? L : 0;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) maxL = max(maxL, __shfl_xor_sync(0xffffffffu, maxL, d));
+        int rank = 0;
+        for (int j = 0; j < maxL; ++j) {
+            int src = (mine ? s : 0) + j;
+            uint32_t kj = __shfl_sync(0xffffffffu, kv, src & 31);
+            if (mine && j < L) rank += (kj < kv || (kj == kv && src < ln)) ? 1 : 0;
+        }
+        if (mine) {
+            __stcs(key + base + s + rank, kv);
+            __stcs(W + base + s + rank, x);
+        } else if (valid) {
+            __stcs(key + k, kv);
+        }
+    }
+}
+
+// Groups of 2..16 slots that cross a multiple of 32: each lies inside the
+// 32-slot window centred on that boundary, where it is ranked as above.
+__global__ void __launch_bounds__(kThreads) k_sort_straddle(const int* __restrict__ d_A, const int* __restrict__ G,
+                                                            uint32_t* __restrict__ key, int* __restrict__ W) {
+    const int A = *d_A;
+    const int ln = (int)lane_id();
+    const int nwin = (A + 31) / 32;  // boundaries at 32, 64, ...
+    const int nwarps = gridDim.x * kWarps;
+    for (int win = blockIdx.x * kWarps + (int)warp_id(); win + 1 < nwin; win += nwarps) {
+        const int base = win * 32 + 16;
+        const int k = base + ln;
+        const bool valid = k < A;
+        int g = valid ? G[k] : -1;
+        int gp = __shfl_up_sync(0xffffffffu, g, 1);
+        if (ln == 0) gp = G[base - 1];
+        int gn = __shfl_down_sync(0xffffffffu, g, 1);
+        if (ln == 31) gn = (k + 1 < A) ? G[k + 1] : -2;
+        const unsigned H = __ballot_sync(0xffffffffu, valid && gp != g);
+        const unsigned T = __ballot_sync(0xffffffffu, valid && (k + 1 >= A || gn != g));
+        // the group holding lane 16 crosses the boundary if it starts below lane 16
+        const unsigned h16 = H & 0x1ffffu;
+        const unsigned t16 = T & 0xffff0000u;
+        const int s = h16 ? 31 - __clz(h16) : -1;
+        const int e = t16 ? __ffs(t16) - 1 : 32;
+        const int L = e - s + 1;
+        if (s < 0 || s >= 16 || e >= 32 || L > kSmallMax) continue;  // uniform across the warp
+        const bool mine = ln >= s && ln <= e;
+        uint32_t kv = mine ? key[k] : 0u;
+        int wv = mine ? W[k] : 0;
+        int rank = 0;
+        for (int j = 0; j < L; ++j) {
+            uint32_t kj = __shfl_sync(0xffffffffu, kv, s + j);
+            if (mine) rank += (kj < kv || (kj == kv && s + j < ln)) ? 1 : 0;
+        }
+        if (mine) {
+            key[base + s + rank] = kv;
+            W[base + s + rank] = wv;
         }
     }
 }
@@ -664,15 +758,16 @@ int grid_for(long long work, int per_cta, int cap) {
 // Sorts every group (key, W) in place in compact slot space.  hc: host copy
 // of the counters (list lengths, slots per class); A: active slots.
 void sort_groups(Storage* S, const int* hc, int A, const int* d_A, uint32_t* key, int* W, const int* G,
-                 cudaStream_t st) {
+                 cudaStream_t st, bool small_done) {
     FwdBuffers& f = S->f;
     int* cnt = S->counters;
     const int sms = S->sms;
     int nmd = hc[CNT_MED], nlg = hc[CNT_LARGE];
     long long small_el = (long long)A - hc[CNT_MED_ELEMS] - hc[CNT_TILE_ELEMS] - hc[CNT_LARGE_ELEMS];
     // every slot: group rank read; small groups: key and suffix read and written
-    QZ_LAUNCH(S, st, "k_sort_small", 12ll * A + 8ll * small_el,
-              k_sort_small<<<grid_for(A, kThreads, sms * 16), kThreads, 0, st>>>(d_A, G, key, W));
+    if (small_el > 0 && !small_done)
+        QZ_LAUNCH(S, st, "k_sort_small", 4ll * A + 16ll * small_el,
+                  k_sort_small<<<grid_for(A, kThreads, sms * 16), kThreads, 0, st>>>(d_A, G, key, W));
     if (nmd > 0)
         QZ_LAUNCH(S, st, "k_sort_medium", 16ll * hc[CNT_MED_ELEMS] + 8ll * nmd,
                   k_sort_medium<<<grid_for(nmd, kWarps, sms * 16), kThreads, 0, st>>>(f.list_med, cnt + CNT_MED,
@@ -793,7 +888,7 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
     int act = CNT_ACTIVE;  // counter slot holding the current active count
     GatherArgs ga{f.R, S->blk_off, nb, S->blk_K, -1};
     // ---- initial sort (groups = blocks)
-    sort_groups(S, cnt0, (int)N, S->counters + act, f.key, f.W[0], f.G[0], st);
+    sort_groups(S, cnt0, (int)N, S->counters + act, f.key, f.W[0], f.G[0], st, false);
     if (dump) {
         dump_array("sorted_key", f.key, 4 * N, st);
         dump_array("sorted_W", f.W[0], 4 * N, st);
@@ -872,11 +967,16 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
         }
         add_round(S, round + 1, A);
         ga.round = round;
-        // reads the suffix, gathers one rank, writes the key
-        QZ_LAUNCH(S, st, "k_gather", 12ll * A,
-                  k_gather<<<grid_for(A, kThreads, S->sms * 16), kThreads, 0, st>>>(S->counters + act, f.W[cur],
-                                                                                    f.key, ga));
-        sort_groups(S, hcnt, A, S->counters + act, f.key, f.W[cur], f.G[cur], st);
+        // suffix and group rank read, one rank gathered, key written; small
+        // groups inside a warp window sorted on the spot (suffix rewritten)
+        long long small_el = (long long)A - hcnt[CNT_MED_ELEMS] - hcnt[CNT_TILE_ELEMS] - hcnt[CNT_LARGE_ELEMS];
+        QZ_LAUNCH(S, st, "k_gather_small", 16ll * A + 4ll * small_el,
+                  k_gather_small<<<grid_for((A + 31) / 32, kWarps, S->sms * 16), kThreads, 0, st>>>(
+                      S->counters + act, f.G[cur], f.key, f.W[cur], ga));
+        QZ_LAUNCH(S, st, "k_sort_straddle", 4ll * A,
+                  k_sort_straddle<<<grid_for((A + 31) / 32, kWarps, S->sms * 16), kThreads, 0, st>>>(
+                      S->counters + act, f.G[cur], f.key, f.W[cur]));
+        sort_groups(S, hcnt, A, S->counters + act, f.key, f.W[cur], f.G[cur], st, true);
         if (dump) {
             dump_array("rsorted_key", f.key, 4 * (size_t)A, st);
             dump_array("rsorted_W", f.W[cur], 4 * (size_t)A, st);

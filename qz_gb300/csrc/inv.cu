@@ -205,6 +205,23 @@ __global__ void __launch_bounds__(kThreads) k_inv_walk2(InvArgs a, RulerArgs r, 
         report(a.st, QZGPU_DATA_CORRUPT, 12, b);
         return;
     }
+    // The walk visits suffixes n-d, n-d-1, ...: a run of consecutive output
+    // bytes written downwards.  Bytes are packed into 32-bit words aligned on
+    // their absolute address, so the run leaves as word stores; a word not
+    // completely filled by this walk is stored byte by byte.
+    uint8_t* out = T + bs;
+    uintptr_t word_at = 0;  // address of the word being filled (0: none)
+    uint32_t word = 0;
+    unsigned have = 0;      // bytes of that word filled so far (bit mask)
+    auto flush = [&]() {
+        if (!have) return;
+        if (have == 0xfu) {
+            *reinterpret_cast<uint32_t*>(word_at) = word;
+        } else {
+            for (int q = 0; q < 4; ++q)
+                if (have & (1u << q)) reinterpret_cast<uint8_t*>(word_at)[q] = (uint8_t)(word >> (8 * q));
+        }
+    };
     for (int t = 0; t < L; ++t) {
         int s = n - d;
         if (s < 0) {
@@ -217,11 +234,22 @@ __global__ void __launch_bounds__(kThreads) k_inv_walk2(InvArgs a, RulerArgs r, 
                 int mid = (lo + hi + 1) >> 1;
                 if (C[mid] <= cur) lo = mid; else hi = mid - 1;
             }
-            T[bs + s] = (uint8_t)lo;
+            uintptr_t addr = reinterpret_cast<uintptr_t>(out + s);
+            uintptr_t wa = addr & ~(uintptr_t)3;
+            if (wa != word_at) {
+                flush();
+                word_at = wa;
+                word = 0;
+                have = 0;
+            }
+            int q = (int)(addr & 3);
+            word |= (uint32_t)lo << (8 * q);
+            have |= 1u << q;
         }
         cur = LF[cur];
         ++d;
     }
+    flush();
 }
 
 int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t* d_U, uint8_t* d_T,

@@ -1,0 +1,196 @@
+// Batched calls on a multi-lane engine.
+//
+// A storage handed to callers (qzgpu_storage) is an engine of K lanes (two by
+// default: measured best on a 33-block chunk; QZGPU_LANES overrides).  Each
+// lane is a full scratch set (Storage) with its own stream and a persistent
+// worker thread.  A batch is cut into sub-batches of at most lane_bytes block
+// bytes (blocks kept whole); lanes take sub-batches as they become free, so
+// the latency-bound phases of one sub-batch (dependent gathers, per-round host
+// reads of the counters) overlap with the work of the others on the device.
+// Lane 0 is sized for the whole capacity and alone takes a block larger than
+// lane_bytes.
+#include <algorithm>
+#include <atomic>
+#include <cstdlib>
+
+#include "engine.h"
+
+namespace qz {
+
+namespace {
+
+int lanes_for(long long cap_bytes) {
+    const char* env = getenv("QZGPU_LANES");
+    if (env && atoi(env) > 0) return std::min(atoi(env), 16);
+    return cap_bytes > kLaneBytes ? 2 : 1;
+}
+
+}  // namespace
+
+size_t engine_device_bytes(long long cap_bytes, int cap_blocks) {
+    int k = lanes_for(cap_bytes);
+    size_t b = storage_device_bytes(cap_bytes, cap_blocks);
+    if (k > 1) b += (size_t)(k - 1) * storage_device_bytes(std::min(cap_bytes, kLaneBytes), cap_blocks);
+    return b;
+}
+
+int engine_init(Engine* E, long long cap_bytes, int cap_blocks) {
+    E->cap_bytes = cap_bytes;
+    E->cap_blocks = cap_blocks;
+    E->lane_bytes = std::min(cap_bytes, kLaneBytes);
+    int k = lanes_for(cap_bytes);
+    for (int i = 0; i < k; ++i) {
+        auto s = std::make_unique<Storage>();
+        int rc = storage_init(s.get(), i == 0 ? cap_bytes : E->lane_bytes, cap_blocks);
+        if (rc) {
+            engine_free(E);
+            return rc;
+        }
+        E->lanes.push_back(std::move(s));
+    }
+    E->device = E->lanes[0]->device;
+    for (int i = 0; i < k; ++i) {
+        E->threads.emplace_back([E, i] {
+            cudaSetDevice(E->device);
+            int seen = 0;
+            for (;;) {
+                std::function<void(int)> job;
+                {
+                    std::unique_lock<std::mutex> lk(E->jmu);
+                    E->jcv.wait(lk, [&] { return E->stop || E->job_gen != seen; });
+                    if (E->stop) return;
+                    seen = E->job_gen;
+                    job = E->job;
+                }
+                job(i);
+                {
+                    std::lock_guard<std::mutex> lk(E->jmu);
+                    ++E->job_done;
+                }
+                E->dcv.notify_all();
+            }
+        });
+    }
+    return QZGPU_NO_ERROR;
+}
+
+void engine_free(Engine* E) {
+    {
+        std::lock_guard<std::mutex> lk(E->jmu);
+        E->stop = true;
+    }
+    E->jcv.notify_all();
+    for (auto& t : E->threads) t.join();
+    E->threads.clear();
+    for (auto& s : E->lanes) {
+        cudaSetDevice(s->device);
+        storage_free(s.get());
+    }
+    E->lanes.clear();
+}
+
+int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned char* const* hin,
+               unsigned char* const* hout, const unsigned char* d_in, unsigned char* d_out, int* idx,
+               cudaStream_t user_stream) {
+    const bool host = hin != nullptr;
+    if (!host && user_stream) {
+        // inputs produced on the caller's stream must be complete
+        cudaError_t e = cudaStreamSynchronize(user_stream);
+        if (e != cudaSuccess) return map_cuda_error(e);
+    }
+    // sub-batches: consecutive whole blocks, at most lane_bytes (a larger block alone)
+    struct Sub {
+        int b0, b1;
+        long long off, bytes;
+    };
+    std::vector<Sub> big, small;
+    long long off = 0;
+    long long limit = E->lane_bytes;
+    if (!forward) {
+        const char* env = getenv("QZGPU_INV_SUB_MB");
+        if (env && atof(env) > 0) limit = std::min(limit, (long long)(atof(env) * (1 << 20)));
+    }
+    for (int b0 = 0; b0 < nb;) {
+        int b1 = b0;
+        long long bytes = 0;
+        while (b1 < nb && (b1 == b0 || bytes + n[b1] <= limit)) bytes += n[b1++];
+        (bytes > E->lane_bytes ? big : small).push_back(Sub{b0, b1, off, bytes});
+        off += bytes;
+        b0 = b1;
+    }
+    const int K = (int)E->lanes.size();
+    std::atomic<int> cursor{0};
+    std::atomic<int> first_err{0};
+    std::vector<std::vector<long long>> lane_rounds(K);
+    std::vector<int> lane_maxr(K, 0), lane_launch(K, 0);
+    for (auto& s : E->lanes) s->profile = E->profile;
+    auto run_sub = [&](int lane, const Sub& sb) {
+        Storage* S = E->lanes[lane].get();
+        const int cnt = sb.b1 - sb.b0;
+        int rc;
+        if (host) {
+            rc = forward ? encode_host(S, cnt, hin + sb.b0, hout + sb.b0, n + sb.b0, idx + sb.b0, nullptr, nullptr)
+                         : decode_host(S, cnt, hin + sb.b0, hout + sb.b0, n + sb.b0, idx + sb.b0);
+        } else {
+            rc = forward ? forward_run(S, cnt, n + sb.b0, d_in + sb.off, d_out + sb.off, idx + sb.b0, nullptr,
+                                       nullptr, S->stream)
+                         : inverse_run(S, cnt, n + sb.b0, idx + sb.b0, d_in + sb.off, d_out + sb.off, S->stream);
+        }
+        if (rc) {
+            int z = 0;
+            first_err.compare_exchange_strong(z, rc);
+            return;
+        }
+        auto& lr = lane_rounds[lane];
+        if (lr.size() < S->rounds_active.size()) lr.resize(S->rounds_active.size(), 0);
+        for (size_t r = 0; r < S->rounds_active.size(); ++r) lr[r] += S->rounds_active[r];
+        lane_maxr[lane] = std::max(lane_maxr[lane], S->stats.rounds);
+        lane_launch[lane] += S->stats.kernel_launches;
+    };
+    {
+        std::unique_lock<std::mutex> lk(E->jmu);
+        E->job = [&](int lane) {
+            cudaSetDevice(E->device);
+            if (lane == 0)
+                for (const Sub& sb : big)
+                    if (!first_err.load()) run_sub(0, sb);
+            for (;;) {
+                int i = cursor.fetch_add(1);
+                if (i >= (int)small.size() || first_err.load()) break;
+                run_sub(lane, small[i]);
+            }
+        };
+        E->job_done = 0;
+        ++E->job_gen;
+        E->jcv.notify_all();
+        E->dcv.wait(lk, [&] { return E->job_done == K; });
+        E->job = nullptr;
+    }
+    // merge lane counters
+    E->stats = qzgpu_stats{};
+    E->rounds_active.clear();
+    long long active = 0;
+    for (int i = 0; i < K; ++i) {
+        auto& lr = lane_rounds[i];
+        if (E->rounds_active.size() < lr.size()) E->rounds_active.resize(lr.size(), 0);
+        for (size_t r = 0; r < lr.size(); ++r) {
+            E->rounds_active[r] += lr[r];
+            active += lr[r];
+        }
+        E->stats.rounds = std::max(E->stats.rounds, lane_maxr[i]);
+        E->stats.kernel_launches += lane_launch[i];
+        for (auto& kv : E->lanes[i]->prof) {
+            auto& g = E->prof[kv.first];
+            g.launches += kv.second.launches;
+            g.ms += kv.second.ms;
+            g.bytes += kv.second.bytes;
+        }
+        E->lanes[i]->prof.clear();
+    }
+    long long N = off;
+    E->stats.active_total = active;
+    E->stats.alg_bytes = forward ? 15 * N + 28 * active : 12 * N;
+    return first_err.load();
+}
+
+}  // namespace qz

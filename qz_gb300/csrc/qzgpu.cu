@@ -354,7 +354,7 @@ void storage_free(Storage* S) {
 
 using namespace qz;
 
-struct qzgpu_storage : public qz::Storage {};
+struct qzgpu_storage : public qz::Engine {};
 
 namespace qz {
 
@@ -521,15 +521,16 @@ int qzgpu_bwt_decode(unsigned char* T, int n, int index, unsigned char num_index
 
 long long qzgpu_storage_bytes(long long max_total_bytes, int max_blocks) {
     if (max_total_bytes < 1 || max_blocks < 1) return 0;
-    return (long long)storage_device_bytes(max_total_bytes, max_blocks);
+    return (long long)engine_device_bytes(max_total_bytes, max_blocks);
 }
 
 int qzgpu_storage_create(qzgpu_storage** storage, long long max_total_bytes, int max_blocks) {
     if (!storage) return QZGPU_BAD_PARAMETER;
     *storage = nullptr;
+    if (max_total_bytes < 1 || max_blocks < 1 || max_total_bytes > QZGPU_MAX_BATCH_BYTES) return QZGPU_BAD_PARAMETER;
     auto* s = new (std::nothrow) qzgpu_storage();
     if (!s) return QZGPU_NOT_ENOUGH_MEMORY;
-    int rc = storage_init(s, max_total_bytes, max_blocks);
+    int rc = engine_init(s, max_total_bytes, max_blocks);
     if (rc) {
         delete s;
         return rc;
@@ -542,62 +543,61 @@ int qzgpu_storage_destroy(qzgpu_storage* storage) {
     if (!storage) return QZGPU_BAD_PARAMETER;
     {
         std::lock_guard<std::mutex> lk(storage->mu);
-        cudaSetDevice(storage->device);
-        storage_free(storage);
+        engine_free(storage);
     }
     delete storage;
     return QZGPU_NO_ERROR;
 }
 
-int qzgpu_bwt_encode_batch(qzgpu_storage* storage, int nblocks, const unsigned char* const* T,
-                           unsigned char* const* U, const int* n, int* indexes, int features) {
-    (void)features;
+namespace {
+
+int engine_call(qzgpu_storage* storage, bool forward, int nblocks, const int* n, const unsigned char* const* hin,
+                unsigned char* const* hout, const unsigned char* d_in, unsigned char* d_out, int* idx, void* stream) {
     long long total;
     int rc = check_blocks(nblocks, n, &total);
     if (rc) return rc;
-    if (!storage || (nblocks > 0 && (!T || !U || !indexes))) return QZGPU_BAD_PARAMETER;
+    if (!storage) return QZGPU_BAD_PARAMETER;
+    bool host = hin != nullptr;
+    if (nblocks > 0 && !idx) return QZGPU_BAD_PARAMETER;
+    if (host && nblocks > 0 && !hout) return QZGPU_BAD_PARAMETER;
+    if (!host && total > 0 && (!d_in || !d_out || d_in == d_out)) return QZGPU_BAD_PARAMETER;
+    if (!forward)
+        for (int b = 0; b < nblocks; ++b)
+            if (n[b] > 0 && (idx[b] < 1 || idx[b] > n[b])) return QZGPU_DATA_CORRUPT;
     std::lock_guard<std::mutex> lk(storage->mu);
     if (total > storage->cap_bytes || nblocks > storage->cap_blocks) return QZGPU_BAD_PARAMETER;
-    return encode_host(storage, nblocks, T, U, n, indexes, nullptr, nullptr);
+    cudaError_t e = cudaSetDevice(storage->device);
+    if (e != cudaSuccess) return map_cuda_error(e);
+    return engine_run(storage, forward, nblocks, n, hin, hout, d_in, d_out, idx,
+                      reinterpret_cast<cudaStream_t>(stream));
+}
+
+}  // namespace
+
+int qzgpu_bwt_encode_batch(qzgpu_storage* storage, int nblocks, const unsigned char* const* T,
+                           unsigned char* const* U, const int* n, int* indexes, int features) {
+    (void)features;
+    if (nblocks > 0 && (!T || !U)) return QZGPU_BAD_PARAMETER;
+    return engine_call(storage, true, nblocks, n, nblocks > 0 ? T : (const unsigned char* const*)&T, U, nullptr,
+                       nullptr, indexes, nullptr);
 }
 
 int qzgpu_bwt_decode_batch(qzgpu_storage* storage, int nblocks, const unsigned char* const* U,
                            unsigned char* const* T, const int* n, const int* indexes, int features) {
     (void)features;
-    long long total;
-    int rc = check_blocks(nblocks, n, &total);
-    if (rc) return rc;
-    if (!storage || (nblocks > 0 && (!T || !U || !indexes))) return QZGPU_BAD_PARAMETER;
-    std::lock_guard<std::mutex> lk(storage->mu);
-    if (total > storage->cap_bytes || nblocks > storage->cap_blocks) return QZGPU_BAD_PARAMETER;
-    return decode_host(storage, nblocks, U, T, n, indexes);
+    if (nblocks > 0 && (!T || !U)) return QZGPU_BAD_PARAMETER;
+    return engine_call(storage, false, nblocks, n, nblocks > 0 ? U : (const unsigned char* const*)&U, T, nullptr,
+                       nullptr, const_cast<int*>(indexes), nullptr);
 }
 
 int qzgpu_bwt_encode_device(qzgpu_storage* storage, int nblocks, const int* n, const unsigned char* d_T,
                             unsigned char* d_U, int* indexes, void* stream) {
-    long long total;
-    int rc = check_blocks(nblocks, n, &total);
-    if (rc) return rc;
-    if (!storage || (total > 0 && (!d_T || !d_U || !indexes)) || d_T == d_U) return QZGPU_BAD_PARAMETER;
-    std::lock_guard<std::mutex> lk(storage->mu);
-    if (total > storage->cap_bytes || nblocks > storage->cap_blocks) return QZGPU_BAD_PARAMETER;
-    cudaError_t e = cudaSetDevice(storage->device);
-    if (e != cudaSuccess) return map_cuda_error(e);
-    return forward_run(storage, nblocks, n, d_T, d_U, indexes, nullptr, nullptr,
-                       reinterpret_cast<cudaStream_t>(stream));
+    return engine_call(storage, true, nblocks, n, nullptr, nullptr, d_T, d_U, indexes, stream);
 }
 
 int qzgpu_bwt_decode_device(qzgpu_storage* storage, int nblocks, const int* n, const int* indexes,
                             const unsigned char* d_U, unsigned char* d_T, void* stream) {
-    long long total;
-    int rc = check_blocks(nblocks, n, &total);
-    if (rc) return rc;
-    if (!storage || (total > 0 && (!d_T || !d_U || !indexes)) || d_T == d_U) return QZGPU_BAD_PARAMETER;
-    std::lock_guard<std::mutex> lk(storage->mu);
-    if (total > storage->cap_bytes || nblocks > storage->cap_blocks) return QZGPU_BAD_PARAMETER;
-    cudaError_t e = cudaSetDevice(storage->device);
-    if (e != cudaSuccess) return map_cuda_error(e);
-    return inverse_run(storage, nblocks, n, indexes, d_U, d_T, reinterpret_cast<cudaStream_t>(stream));
+    return engine_call(storage, false, nblocks, n, nullptr, nullptr, d_U, d_T, const_cast<int*>(indexes), stream);
 }
 
 int qzgpu_storage_round_counts(const qzgpu_storage* storage, long long* active, int max) {
