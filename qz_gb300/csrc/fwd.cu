@@ -351,71 +351,66 @@ __global__ void __launch_bounds__(kThreads) k_sort_straddle(const int* __restric
     }
 }
 
-// Groups of 17..512 slots: one warp per listed group, bitonic sort across
-// lanes in registers (element e = lane + 32 r, M registers per lane).
-template <int M>
-__device__ __forceinline__ void warp_sort_group(int s, int len, uint32_t* key, int* W) {
-    const int ln = (int)lane_id();
-    unsigned long long v[M];
-#pragma unroll
-    for (int r = 0; r < M; ++r) {
-        int e = ln + 32 * r;
-        v[r] = e < len ? pack_kv(key[s + e], W[s + e]) : ~0ull;
-    }
-#pragma unroll
-    for (int k = 2; k <= 32 * M; k <<= 1) {
-#pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            if (j >= 32) {
-                const int jr = j / 32;
-#pragma unroll
-                for (int r = 0; r < M; ++r) {
-                    int pr = r ^ jr;
-                    if (pr > r) {
-                        int e = ln + 32 * r;
-                        bool up = (e & k) == 0;
-                        unsigned long long x = v[r], y = v[pr];
-                        bool sw = up ? (x > y) : (x < y);
-                        v[r] = sw ? y : x;
-                        v[pr] = sw ? x : y;
-                    }
-                }
-            } else {
-#pragma unroll
-                for (int r = 0; r < M; ++r) {
-                    int e = ln + 32 * r;
-                    unsigned long long y = __shfl_xor_sync(0xffffffffu, v[r], j);
-                    bool lower = (ln & j) == 0;
-                    bool up = (e & k) == 0;
-                    unsigned long long mn = v[r] < y ? v[r] : y;
-                    unsigned long long mx = v[r] < y ? y : v[r];
-                    v[r] = (lower == up) ? mn : mx;
-                }
-            }
-        }
-    }
-#pragma unroll
-    for (int r = 0; r < M; ++r) {
-        int e = ln + 32 * r;
-        if (e < len) {
-            key[s + e] = (uint32_t)(v[r] >> 32);
-            W[s + e] = (int)(uint32_t)v[r];
-        }
-    }
-}
-
+// Groups of 17..512 slots, one warp per listed group.  Up to 64 slots: two
+// slots per lane, each ranks itself by counting smaller keys (ties by slot)
+// over shuffled keys.  65..512 slots: a bitonic sort in the warp's share of
+// shared memory (loops, not unrolled, so the kernel stays small).
 __global__ void __launch_bounds__(kThreads) k_sort_medium(const int2* __restrict__ list,
                                                           const int* __restrict__ d_count,
                                                           uint32_t* __restrict__ key, int* __restrict__ W) {
+    __shared__ unsigned long long buf[kWarps][kMedMax];
     int cnt = *d_count;
-    int nwarps = gridDim.x * kWarps;
+    const int nwarps = gridDim.x * kWarps;
+    const int ln = (int)lane_id();
+    unsigned long long* sb = buf[warp_id()];
     for (int i = blockIdx.x * kWarps + (int)warp_id(); i < cnt; i += nwarps) {
         int2 d = list[i];
-        if (d.y <= 32) warp_sort_group<1>(d.x, d.y, key, W);
-        else if (d.y <= 64) warp_sort_group<2>(d.x, d.y, key, W);
-        else if (d.y <= 128) warp_sort_group<4>(d.x, d.y, key, W);
-        else if (d.y <= 256) warp_sort_group<8>(d.x, d.y, key, W);
-        else warp_sort_group<16>(d.x, d.y, key, W);
+        const int s = d.x, len = d.y;
+        if (len <= 64) {
+            bool v0 = ln < len, v1 = ln + 32 < len;
+            uint32_t k0 = v0 ? key[s + ln] : 0xffffffffu, k1 = v1 ? key[s + ln + 32] : 0xffffffffu;
+            int w0 = v0 ? W[s + ln] : 0, w1 = v1 ? W[s + ln + 32] : 0;
+            int r0 = 0, r1 = 0;
+            for (int j = 0; j < len; ++j) {
+                uint32_t kj = __shfl_sync(0xffffffffu, j < 32 ? k0 : k1, j & 31);
+                r0 += (kj < k0 || (kj == k0 && j < ln)) ? 1 : 0;
+                r1 += (kj < k1 || (kj == k1 && j < ln + 32)) ? 1 : 0;
+            }
+            if (v0) {
+                key[s + r0] = k0;
+                W[s + r0] = w0;
+            }
+            if (v1) {
+                key[s + r1] = k1;
+                W[s + r1] = w1;
+            }
+            continue;
+        }
+        int np = 128;
+        while (np < len) np <<= 1;
+        for (int j = ln; j < np; j += 32) sb[j] = j < len ? pack_kv(key[s + j], W[s + j]) : ~0ull;
+        __syncwarp();
+        for (int k = 2; k <= np; k <<= 1) {
+            for (int jj = k >> 1; jj > 0; jj >>= 1) {
+                for (int a = ln; a < np; a += 32) {
+                    int l = a ^ jj;
+                    if (l > a) {
+                        unsigned long long x = sb[a], y = sb[l];
+                        bool up = (a & k) == 0;
+                        if (up ? (x > y) : (x < y)) {
+                            sb[a] = y;
+                            sb[l] = x;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        for (int j = ln; j < len; j += 32) {
+            key[s + j] = (uint32_t)(sb[j] >> 32);
+            W[s + j] = (int)(uint32_t)sb[j];
+        }
+        __syncwarp();
     }
 }
 
@@ -469,17 +464,20 @@ struct SplitArgs {
 struct WarpTile {
     uint32_t k[kWI];
     int g[kWI];
+    int w[kWI];
     bool valid[kWI], gh[kWI], sh[kWI], nsh[kWI];
 };
 
+template <bool WithSuffix>
 __device__ __forceinline__ void wt_load(const SplitArgs& a, int A, int base, WarpTile& t) {
     const unsigned ln = lane_id();
 #pragma unroll
     for (int i = 0; i < kWI; ++i) {
         int kk = base + 32 * i + (int)ln;
         t.valid[i] = kk < A;
-        t.k[i] = t.valid[i] ? a.key[kk] : 0u;
-        t.g[i] = t.valid[i] ? a.G[kk] : -1;
+        t.k[i] = t.valid[i] ? __ldcs(a.key + kk) : 0u;
+        t.g[i] = t.valid[i] ? __ldcs(a.G + kk) : -1;
+        if (WithSuffix) t.w[i] = t.valid[i] ? __ldcs(a.W + kk) : 0;
     }
     uint32_t pk = 0, nk = 0;
     int pg = -1, ng = -1;
@@ -527,7 +525,7 @@ __global__ void __launch_bounds__(kThreads) k_split_count(SplitArgs a) {
     for (int tile = blockIdx.x * kWarps + (int)warp_id(); tile < ntiles; tile += nwarps) {
         int base = tile * kWT;
         WarpTile t;
-        wt_load(a, A, base, t);
+        wt_load<false>(a, A, base, t);
         uint32_t surv = 0;
         int sub = -1, grp = -1;
 #pragma unroll
@@ -656,7 +654,7 @@ __global__ void __launch_bounds__(kThreads) k_pscan_apply(SplitArgs a, const uin
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_split_apply(SplitArgs a) {
+__global__ void __launch_bounds__(kThreads, 5) k_split_apply(SplitArgs a) {
     int A = *a.A;
     int ntiles = (A + kWT - 1) / kWT;
     int nwarps = gridDim.x * kWarps;
@@ -665,7 +663,7 @@ __global__ void __launch_bounds__(kThreads) k_split_apply(SplitArgs a) {
     for (int tile = blockIdx.x * kWarps + (int)warp_id(); tile < ntiles; tile += nwarps) {
         int base = tile * kWT;
         WarpTile t;
-        wt_load(a, A, base, t);
+        wt_load<true>(a, A, base, t);
         uint32_t dest = a.p_surv[tile];
         int csub = a.p_sub[tile], cgrp = a.p_grp[tile];
 #pragma unroll
@@ -683,7 +681,7 @@ __global__ void __launch_bounds__(kThreads) k_split_apply(SplitArgs a) {
             uint32_t d = dest + __popc(m & lt_mask);
             dest += __popc(m);
             if (t.valid[i]) {
-                int w = __ldcs(a.W + kk);
+                int w = t.w[i];
                 int g = t.g[i];
                 int rank = g + (ks - kg);
                 if (a.write_all || rank != g) a.R[w] = rank;
