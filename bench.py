@@ -254,6 +254,7 @@ def run_gpu(args, rank: int, world: int):
     for k in range(args.steps):
         idx = st.encode_device(sizes, d_T.data_ptr(), d_U.data_ptr(), sptr)
         fwd_stats = st.stats()
+        rounds_active = st.round_counts()
         launches += fwd_stats["kernel_launches"]
         ev[3 * k + 1].record(stream)
         st.decode_device(sizes, idx, d_U.data_ptr(), d_R.data_ptr(), sptr)
@@ -269,7 +270,6 @@ def run_gpu(args, rank: int, world: int):
     inv_ms = sum(ev[3 * k + 1].elapsed_time(ev[3 * k + 2]) for k in range(args.steps))
     prof = st.profile_read(reset=True)
     st.profile(False)
-    rounds_active = st.round_counts()
     if dist:
         t = torch.tensor([total_ms, fwd_ms, inv_ms], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)

@@ -141,11 +141,12 @@ int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned cha
             first_err.compare_exchange_strong(z, rc);
             return;
         }
+        lane_launch[lane] += S->stats.kernel_launches;
+        if (!forward) return;  // round counts describe forward calls only
         auto& lr = lane_rounds[lane];
         if (lr.size() < S->rounds_active.size()) lr.resize(S->rounds_active.size(), 0);
         for (size_t r = 0; r < S->rounds_active.size(); ++r) lr[r] += S->rounds_active[r];
         lane_maxr[lane] = std::max(lane_maxr[lane], S->stats.rounds);
-        lane_launch[lane] += S->stats.kernel_launches;
     };
     {
         std::unique_lock<std::mutex> lk(E->jmu);
@@ -166,9 +167,9 @@ int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned cha
         E->dcv.wait(lk, [&] { return E->job_done == K; });
         E->job = nullptr;
     }
-    // merge lane counters
+    // merge lane counters (round counts only for a forward call)
     E->stats = qzgpu_stats{};
-    E->rounds_active.clear();
+    if (forward) E->rounds_active.clear();
     long long active = 0;
     for (int i = 0; i < K; ++i) {
         auto& lr = lane_rounds[i];
