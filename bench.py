@@ -232,6 +232,22 @@ def run_gpu(args, rank: int, world: int):
         st.decode_device(sizes, idx, d_U.data_ptr(), d_R.data_ptr(), sptr)
         return idx, fl + st.stats()["kernel_launches"]
 
+    # ---- autotuner (before warm-up; not timed)
+    tuned = None
+    if not args.no_autotune:
+        from qz_gb300 import autotune
+
+        def run_once():
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            return e0.elapsed_time(e1)
+
+        run_once()
+        key = autotune.signature(blocks, torch.cuda.get_device_name(dev))
+        tuned = autotune.tune(st, run_once, key=key, use_cache=False)
     for _ in range(args.warmup):
         idx, _ = step()
     torch.cuda.synchronize(dev)
@@ -368,6 +384,7 @@ def run_gpu(args, rank: int, world: int):
             "config": {"workload": desc, "blocks": len(blocks), "bytes": N,
                        "l2": "inputs larger than L2 (workload bytes and scratch exceed 126 MB)",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "tuned": tuned if tuned else st.params(),
                        "step": "forward BWT of all blocks + inverse BWT of the result"},
             "fwd_mb_s": round(world * N * args.steps / (fwd_ms / 1e3) / 1e6, 3),
             "inv_mb_s": round(world * N * args.steps / (inv_ms / 1e3) / 1e6, 3),
@@ -499,6 +516,7 @@ def main():
     ap.add_argument("--reads", type=int, default=2_500_000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the library's default knobs")
     ap.add_argument("--plain-blocks", action="store_true",
                     help="also time the plain path: one forward + inverse call per block")
     args = ap.parse_args()

@@ -141,6 +141,17 @@ int qzgpu_storage_last_stats(const qzgpu_storage *storage, qzgpu_stats *out);
  * doubling round r).  Copies up to `max` entries; returns how many exist. */
 int qzgpu_storage_round_counts(const qzgpu_storage *storage, long long *active, int max);
 
+/* Runtime tuning of a storage (set by the autotuner, qz_gb300/autotune.py):
+ *   "fwd_sub_bytes", "inv_sub_bytes"  block bytes per sub-batch taken by a lane
+ *   "big_ctas_per_sm"                 persistent CTAs per SM of a radix pass (1..4)
+ *   "tile_ctas_per_sm"                CTAs per SM of the one-CTA group sort (1..3)
+ *   "medium_max"                      longest group sorted by one warp (64..512)
+ *   "ruler_stride_log2"               inverse: a ruler every 2^v rows (3..7)
+ * get_param also answers "lanes".  Returns 0 / the value, or QZGPU_BAD_PARAMETER
+ * for an unknown name or an out-of-range value.  No counterpart in libbsc. */
+int qzgpu_storage_set_param(qzgpu_storage *storage, const char *name, long long value);
+long long qzgpu_storage_get_param(const qzgpu_storage *storage, const char *name);
+
 /* Per-kernel timing of later calls on a storage: when enabled, every launch
  * is bracketed by CUDA events on the stream it runs on.  Diagnostic only; no
  * counterpart in libbsc. */

@@ -107,6 +107,18 @@ class Storage:
         return {"rounds": s.rounds, "kernel_launches": s.kernel_launches, "active_total": s.active_total,
                 "alg_bytes": s.alg_bytes}
 
+    PARAMS = ("fwd_sub_bytes", "inv_sub_bytes", "big_ctas_per_sm", "tile_ctas_per_sm", "medium_max",
+              "ruler_stride_log2")
+
+    def set_param(self, name: str, value: int) -> None:
+        check(self._lib.qzgpu_storage_set_param(self._h, name.encode(), int(value)), f"set_param({name})")
+
+    def get_param(self, name: str) -> int:
+        return check(self._lib.qzgpu_storage_get_param(self._h, name.encode()), f"get_param({name})")
+
+    def params(self) -> dict:
+        return {k: self.get_param(k) for k in self.PARAMS + ("lanes",)}
+
     def round_counts(self) -> list[int]:
         """Suffixes sorted per round of the last forward call (entry 0 = all)."""
         buf = (ctypes.c_longlong * 64)()

@@ -76,7 +76,16 @@ struct InvBuffers {
     int2* rtiles;   // (block, first ruler) per walk tile
 };
 
+// Runtime tuning knobs of a lane (set through qzgpu_storage_set_param).
+struct Tune {
+    int big_ctas_per_sm = 4;   // persistent CTAs of a look-back radix pass
+    int tile_ctas_per_sm = 3;  // CTAs of the one-CTA group sort
+    int medium_max = kMedMax;  // longest group sorted by one warp (64..512)
+    int ruler_log2 = 5;        // inverse: a ruler every 2^ruler_log2 rows (3..7)
+};
+
 struct Storage {
+    Tune tune;
     long long cap_bytes = 0;
     int cap_blocks = 0;
     int device = 0;
@@ -162,6 +171,8 @@ struct Engine {
     int job_gen = 0, job_done = 0;
     bool stop = false;
     bool profile = false;
+    long long fwd_sub_bytes = kLaneBytes;  // forward sub-batch size (<= lane_bytes)
+    long long inv_sub_bytes = kLaneBytes;  // inverse sub-batch size (<= lane_bytes)
     qzgpu_stats stats{};
     std::vector<long long> rounds_active;
     std::map<std::string, Storage::ProfAgg> prof;

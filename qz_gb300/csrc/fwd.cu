@@ -459,6 +459,7 @@ struct SplitArgs {
     int* p_sub;
     int* p_grp;
     int write_all;     // first split: no previous ranks to keep
+    int medium_max;    // longest group listed for the one-warp sort
 };
 
 struct WarpTile {
@@ -694,7 +695,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_split_apply(SplitArgs a) {
                         int L = kk - ks + 1;
                         if (L > kSmallMax) {
                             int2 dsc = make_int2((int)d - L + 1, L);
-                            if (L <= kMedMax) {
+                            if (L <= a.medium_max) {
                                 a.list_med[atomicAdd(&a.counters[CNT_MED], 1)] = dsc;
                                 atomicAdd(&a.counters[CNT_MED_ELEMS], L);
                             } else if (L <= kOT) {
@@ -806,7 +807,7 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
     for (int b = 0; b < nb; ++b) {
         if (n[b] <= kSmallMax) continue;
         int2 dsc = make_int2(off[b], n[b]);
-        if (n[b] <= kMedMax) {
+        if (n[b] <= S->tune.medium_max) {
             l1.push_back(dsc);
             cnt0[CNT_MED_ELEMS] += n[b];
         } else if (n[b] <= kOT) {
@@ -910,6 +911,7 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
         a.p_sub = f.p_sub;
         a.p_grp = f.p_grp;
         a.write_all = first ? 1 : 0;
+        a.medium_max = S->tune.medium_max;
         int grid = grid_for((A + kWT - 1) / kWT, kWarps, S->sms * 8);
         long long tiles_n = (A + kWT - 1) / kWT;
         // count: key and group rank of every slot; 12 bytes of partials per tile

@@ -265,7 +265,7 @@ int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t*
     S->stats = qzgpu_stats{};
     S->launches = 0;
     if (N == 0) return QZGPU_NO_ERROR;
-    const int stride_log2 = 5;  // rulers every 32 rows
+    const int stride_log2 = S->tune.ruler_log2;  // rulers every 2^stride_log2 rows
     const int stride = 1 << stride_log2;
 
     std::vector<int> off(nb + 1, 0), tbase(nb + 1, 0), rbase(nb + 1, 0);

@@ -105,11 +105,7 @@ int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned cha
     };
     std::vector<Sub> big, small;
     long long off = 0;
-    long long limit = E->lane_bytes;
-    if (!forward) {
-        const char* env = getenv("QZGPU_INV_SUB_MB");
-        if (env && atof(env) > 0) limit = std::min(limit, (long long)(atof(env) * (1 << 20)));
-    }
+    long long limit = std::min(E->lane_bytes, forward ? E->fwd_sub_bytes : E->inv_sub_bytes);
     for (int b0 = 0; b0 < nb;) {
         int b1 = b0;
         long long bytes = 0;

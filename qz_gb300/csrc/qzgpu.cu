@@ -140,7 +140,7 @@ Caps caps_for(long long cap_bytes, int cap_blocks) {
     size_t fwd_tiles = 2 * (c.N / kOT) + 2;
     c.hist = 256 * std::max(fwd_tiles, c.init_tiles);
     c.med = c.N / (kSmallMax + 1) + 1;
-    c.tile = c.N / (kMedMax + 1) + 2;
+    c.tile = c.N / 65 + 2;  // medium_max may be tuned down to 64
     c.large = c.N / (kOT + 1) + 2;
     c.big_tiles = 2 * (c.N / kOT) + 2;
     c.rulers = (c.N >> kMinStrideLog2) + c.nb + 1;
@@ -598,6 +598,48 @@ int qzgpu_bwt_encode_device(qzgpu_storage* storage, int nblocks, const int* n, c
 int qzgpu_bwt_decode_device(qzgpu_storage* storage, int nblocks, const int* n, const int* indexes,
                             const unsigned char* d_U, unsigned char* d_T, void* stream) {
     return engine_call(storage, false, nblocks, n, nullptr, nullptr, d_U, d_T, const_cast<int*>(indexes), stream);
+}
+
+int qzgpu_storage_set_param(qzgpu_storage* storage, const char* name, long long value) {
+    if (!storage || !name) return QZGPU_BAD_PARAMETER;
+    std::lock_guard<std::mutex> lk(storage->mu);
+    std::string k(name);
+    auto each = [&](auto fn) {
+        for (auto& l : storage->lanes) fn(l->tune);
+    };
+    if (k == "fwd_sub_bytes" || k == "inv_sub_bytes") {
+        if (value < (1 << 20)) return QZGPU_BAD_PARAMETER;
+        (k[0] == 'f' ? storage->fwd_sub_bytes : storage->inv_sub_bytes) = value;
+    } else if (k == "big_ctas_per_sm") {
+        if (value < 1 || value > 4) return QZGPU_BAD_PARAMETER;  // all CTAs must stay resident
+        each([&](Tune& t) { t.big_ctas_per_sm = (int)value; });
+    } else if (k == "tile_ctas_per_sm") {
+        if (value < 1 || value > 3) return QZGPU_BAD_PARAMETER;
+        each([&](Tune& t) { t.tile_ctas_per_sm = (int)value; });
+    } else if (k == "medium_max") {
+        if (value != 64 && value != 128 && value != 256 && value != 512) return QZGPU_BAD_PARAMETER;
+        each([&](Tune& t) { t.medium_max = (int)value; });
+    } else if (k == "ruler_stride_log2") {
+        if (value < 3 || value > 7) return QZGPU_BAD_PARAMETER;
+        each([&](Tune& t) { t.ruler_log2 = (int)value; });
+    } else {
+        return QZGPU_BAD_PARAMETER;
+    }
+    return QZGPU_NO_ERROR;
+}
+
+long long qzgpu_storage_get_param(const qzgpu_storage* storage, const char* name) {
+    if (!storage || !name || storage->lanes.empty()) return QZGPU_BAD_PARAMETER;
+    std::string k(name);
+    const Tune& t = storage->lanes[0]->tune;
+    if (k == "fwd_sub_bytes") return storage->fwd_sub_bytes;
+    if (k == "inv_sub_bytes") return storage->inv_sub_bytes;
+    if (k == "big_ctas_per_sm") return t.big_ctas_per_sm;
+    if (k == "tile_ctas_per_sm") return t.tile_ctas_per_sm;
+    if (k == "medium_max") return t.medium_max;
+    if (k == "ruler_stride_log2") return t.ruler_log2;
+    if (k == "lanes") return (long long)storage->lanes.size();
+    return QZGPU_BAD_PARAMETER;
 }
 
 int qzgpu_storage_round_counts(const qzgpu_storage* storage, long long* active, int max) {

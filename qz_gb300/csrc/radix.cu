@@ -312,7 +312,7 @@ void sort_tile_groups(Storage* S, const int2* list, const int* d_count, int host
     if (host_count <= 0) return;
     cudaFuncSetAttribute(k_tile_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_sort_smem());
     QZ_LAUNCH(S, st, "k_tile_sort", 16 * elems,
-              k_tile_sort<<<grid_cap(host_count, 1, S->sms * 3), kThreads, tile_sort_smem(), st>>>(list, d_count,
+              k_tile_sort<<<grid_cap(host_count, 1, S->sms * S->tune.tile_ctas_per_sm), kThreads, tile_sort_smem(), st>>>(list, d_count,
                                                                                                   key, val));
 }
 
@@ -339,7 +339,7 @@ void sort_big_groups(Storage* S, const int2* list, const int* d_count, int host_
     int* dv[4] = {f.wsv[0], f.wsv[1], f.wsv[0], val};
     // persistent grid of resident CTAs (64 registers and 43 KB of shared
     // memory per CTA fit four per SM); tiles are taken by ticket
-    int pgrid = sms * 4;
+    int pgrid = sms * S->tune.big_ctas_per_sm;
     for (int pass = 0; pass < 4; ++pass) {
         unsigned epoch = ++S->radix_epoch & 0x3fffffffu;
         if (epoch == 0) epoch = ++S->radix_epoch & 0x3fffffffu;

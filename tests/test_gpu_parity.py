@@ -150,3 +150,28 @@ def test_decode_wrong_index_does_not_hang(gpu):
         assert len(out) == len(t)
     except native.QzGpuError as e:
         assert e.code == native.QZGPU_DATA_CORRUPT
+
+
+@pytest.mark.parametrize("params", [
+    {"medium_max": 64, "big_ctas_per_sm": 2, "ruler_stride_log2": 3},
+    {"medium_max": 128, "tile_ctas_per_sm": 1, "ruler_stride_log2": 7, "fwd_sub_bytes": 1 << 20,
+     "inv_sub_bytes": 1 << 20},
+    {"medium_max": 256, "big_ctas_per_sm": 1, "ruler_stride_log2": 4},
+])
+def test_tuned_knobs_keep_results(gpu, oracle, params):
+    rng = np.random.default_rng(99)
+    blocks = [synth.sample_reads(synth.uniform_genome(30_000, seed=71), 1500, seed=72),
+              synth.quality_stream(4000, seed=73), synth.header_stream(6000, seed=74),
+              np.resize(np.frombuffer(b"ACG", np.uint8), 90_000), rng.integers(0, 256, 5000).astype(np.uint8)]
+    with bwt.Storage(sum(len(b) for b in blocks), len(blocks)) as st:
+        for k, v in params.items():
+            st.set_param(k, v)
+            assert st.get_param(k) == v
+        us, idx = st.encode_batch(blocks)
+        ous, oidx = oracle.bwt_encode_batch(blocks)
+        assert idx == list(oidx)
+        assert all((u == ou).all() for u, ou in zip(us, ous))
+        back = st.decode_batch(us, idx)
+        assert all((x == y).all() for x, y in zip(back, blocks))
+        with pytest.raises(native.QzGpuError):
+            st.set_param("medium_max", 100)
