@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(kThreads) k_init_keys(const uint8_t* __restric
                                                         const int* __restrict__ Kb,
                                                         const int* __restrict__ sigb,
                                                         uint32_t* __restrict__ key, int* __restrict__ W,
-                                                        int* __restrict__ G) {
+                                                        int* __restrict__ G, uint32_t* __restrict__ R) {
     __shared__ uint8_t scode[256];
     __shared__ uint8_t stext[kInitTile + 64];
     int2 tl = tiles[blockIdx.x];
@@ -113,6 +113,7 @@ __global__ void __launch_bounds__(kThreads) k_init_keys(const uint8_t* __restric
             k = k * (unsigned)sigma + c;
         }
         key[x] = (uint32_t)k;
+        R[x] = (uint32_t)k;
         W[x] = x;
         G[x] = bstart;
     }
@@ -122,8 +123,17 @@ __global__ void __launch_bounds__(kThreads) k_init_keys(const uint8_t* __restric
 
 // Secondary key of suffix x in doubling round `round` (h = K_b << round):
 // R[x+h] + h + 1 when x+h is inside the block, else the remaining length
-// (n_b - i), which is <= h and orders the shorter suffix first.  round < 0:
-// the key was computed from the text (initial sort) and is read from `key`.
+// (n_b - i), which is <= h and orders the shorter suffix first.
+//
+// Round 0 reads text keys instead of ranks: R still holds the K_b-symbol key
+// of every position (written by the initial key pass, not yet overwritten by
+// any split), so the secondary key is R[x+h] itself, and a suffix that ends
+// inside the window gets 0.  The key of x+h orders like its rank did; an
+// ending suffix ties only with suffixes of its group whose next K_b symbols
+// are all the smallest symbol (or padding).  Those ties form the first
+// subgroup of the group in true suffix order and are broken by the end keys
+// of the next round.  A block whose window covers it whole (h >= n_b: one
+// symbol, or a block shorter than K_b) keeps the remaining-length key.
 struct GatherArgs {
     const int* R;
     const int* off;
@@ -149,6 +159,10 @@ __device__ __forceinline__ BlockSpan block_span(const GatherArgs& g, int x) {
 
 __device__ __forceinline__ uint32_t rank_key(const GatherArgs& g, const BlockSpan& s, int x) {
     int i = x - s.bs;
+    if (g.round == 0) {
+        if ((long long)i + s.h < s.n) return (uint32_t)__ldg(g.R + x + (int)s.h);
+        return s.h >= s.n ? (uint32_t)(s.n - i) : 0u;
+    }
     if ((long long)i + s.h < s.n) return (uint32_t)__ldg(g.R + x + (int)s.h) + (uint32_t)s.h + 1u;
     return (uint32_t)(s.n - i);
 }
@@ -414,17 +428,6 @@ __global__ void __launch_bounds__(kThreads) k_sort_medium(const int2* __restrict
     }
 }
 
-// All active slots: the secondary key of each suffix (one rank gathered).
-__global__ void __launch_bounds__(kThreads) k_gather(const int* __restrict__ d_A, const int* __restrict__ W,
-                                                     uint32_t* __restrict__ key, GatherArgs ga) {
-    int A = *d_A;
-    for (int k = blockIdx.x * kThreads + threadIdx.x; k < A; k += gridDim.x * kThreads) {
-        int x = __ldcs(W + k);
-        BlockSpan bsp = block_span(ga, x);
-        __stcs(key + k, rank_key(ga, bsp, x));
-    }
-}
-
 // ------------------------------------------------------------------ split into groups
 //
 // After a sort, slot k (compact, SA order) holds suffix W[k] of group G[k]
@@ -439,6 +442,11 @@ __global__ void __launch_bounds__(kThreads) k_gather(const int* __restrict__ d_A
 // in order, into the next round's slot arrays.
 
 constexpr int kWT = 256;  // slots per warp tile
+
+// Rank writes of a split.  The initial split writes none (R keeps the text
+// keys that round 0 gathers); round 0's split writes every slot's rank; later
+// splits write the ranks that changed.
+constexpr int kRankNone = 0, kRankChanged = 1, kRankAll = 2;
 constexpr int kWI = kWT / 32;
 
 struct SplitArgs {
@@ -458,7 +466,7 @@ struct SplitArgs {
     uint32_t* p_surv;  // per warp tile; exclusive prefix after the partial scan
     int* p_sub;
     int* p_grp;
-    int write_all;     // first split: no previous ranks to keep
+    int write_rank;    // kRankNone / kRankChanged / kRankAll
     int medium_max;    // longest group listed for the one-warp sort
 };
 
@@ -685,7 +693,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_split_apply(SplitArgs a) {
                 int w = t.w[i];
                 int g = t.g[i];
                 int rank = g + (ks - kg);
-                if (a.write_all || rank != g) a.R[w] = rank;
+                if (a.write_rank == kRankAll || (a.write_rank == kRankChanged && rank != g)) a.R[w] = rank;
                 if (single) {
                     a.SA[g + (kk - kg)] = w;
                 } else {
@@ -710,6 +718,17 @@ __global__ void __launch_bounds__(kThreads, 5) k_split_apply(SplitArgs a) {
                 }
             }
         }
+    }
+}
+
+// Ranks of the suffixes the initial split finished.  That split writes no
+// ranks (R holds the text keys round 0 gathers), so once round 0 has gathered,
+// every suffix-array entry it set (the others still hold -1) gives its suffix
+// its final rank: the entry's position.
+__global__ void __launch_bounds__(kThreads) k_rank_fixup(int N, const int* __restrict__ SA, int* __restrict__ R) {
+    for (int j = blockIdx.x * kThreads + threadIdx.x; j < N; j += gridDim.x * kThreads) {
+        int s = __ldcs(SA + j);
+        if (s >= 0) R[s] = j;
     }
 }
 
@@ -873,10 +892,14 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
               k_block_hist<<<ntiles, kThreads, 0, st>>>(d_T, S->tiles, S->blk_off, S->blk_hist));
     QZ_LAUNCH(S, st, "k_block_alpha", 1280ll * nb,
               k_block_alpha<<<nb, kThreads, 0, st>>>(S->blk_hist, S->blk_code, S->blk_K, S->blk_sigma));
-    // reads T once, writes key, W and G
-    QZ_LAUNCH(S, st, "k_init_keys", 13 * N,
+    // reads T once, writes key, R (the same text key, in text order), W and G
+    QZ_LAUNCH(S, st, "k_init_keys", 17 * N,
               k_init_keys<<<ntiles, kThreads, 0, st>>>(d_T, S->tiles, S->blk_off, S->blk_code, S->blk_K,
-                                                       S->blk_sigma, f.key, f.W[0], f.G[0]));
+                                                       S->blk_sigma, f.key, f.W[0], f.G[0],
+                                                       reinterpret_cast<uint32_t*>(f.R)));
+    // suffix-array entries not set by the initial split stay -1 for the fixup
+    e = cudaMemsetAsync(f.SA, 0xff, sizeof(int) * N, st);
+    if (e != cudaSuccess) return map_cuda_error(e);
     const bool dump = dump_on() && N <= (1 << 20);
     if (dump) {
         dump_array("init_key", f.key, 4 * N, st);
@@ -892,7 +915,7 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
         dump_array("sorted_key", f.key, 4 * N, st);
         dump_array("sorted_W", f.W[0], 4 * N, st);
     }
-    auto split = [&](long long A, bool first) {
+    auto split = [&](long long A, int rank_mode) {
         SplitArgs a;
         a.A = S->counters + act;
         a.A_next = S->counters + (act ^ (CNT_ACTIVE ^ CNT_ACTIVE_ALT));
@@ -910,7 +933,7 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
         a.p_surv = f.p_surv;
         a.p_sub = f.p_sub;
         a.p_grp = f.p_grp;
-        a.write_all = first ? 1 : 0;
+        a.write_rank = rank_mode;
         a.medium_max = S->tune.medium_max;
         int grid = grid_for((A + kWT - 1) / kWT, kWarps, S->sms * 8);
         long long tiles_n = (A + kWT - 1) / kWT;
@@ -922,9 +945,9 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
                   k_pscan_top<<<1, kThreads, 0, st>>>(a, f.c_surv, f.c_sub, f.c_grp, kScanGrid));
         QZ_LAUNCH(S, st, "k_pscan_apply", 24 * tiles_n,
                   k_pscan_apply<<<kScanGrid, kThreads, 0, st>>>(a, f.c_surv, f.c_sub, f.c_grp));
-        // apply: key, group, suffix in; rank out where it changed; then the
+        // apply: key, group, suffix in; ranks out per rank_mode; then the
         // suffix either leaves (SA) or is compacted (2 words); fixed up below
-        QZ_LAUNCH(S, st, first ? "k_split_apply_first" : "k_split_apply", 12 * A + 12 * tiles_n,
+        QZ_LAUNCH(S, st, rank_mode == kRankNone ? "k_split_apply_first" : "k_split_apply", 12 * A + 12 * tiles_n,
                   k_split_apply<<<grid, kThreads, 0, st>>>(a));
         cur ^= 1;
         act ^= CNT_ACTIVE ^ CNT_ACTIVE_ALT;
@@ -937,26 +960,32 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
         dump_array("split_W", f.W[cur], 4 * N, st);
         dump_array("split_G", f.G[cur], 4 * N, st);
     };
-    split(N, true);
+    split(N, kRankNone);
     dump_split();
     add_round(S, 0, N);
 
     int* hcnt = S->pin_rd;
     int round = 0;
     long long A_prev = N;
-    bool first_split = true;
+    int last_mode = kRankNone;
+    bool fixed_up = false;
+    auto rank_fixup = [&](long long finished) {
+        // SA read; one rank written per suffix the initial split finished
+        QZ_LAUNCH(S, st, "k_rank_fixup", 4 * N + 4 * finished,
+                  k_rank_fixup<<<grid_for(N, kThreads, S->sms * 16), kThreads, 0, st>>>((int)N, f.SA, f.R));
+        fixed_up = true;
+    };
     for (;;) {
         e = cudaMemcpyAsync(hcnt, S->counters, sizeof(int) * CNT_SLOTS, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return map_cuda_error(e);
         int A = hcnt[act];
         // the last split wrote A survivors (8 B) and A_prev - A suffix-array
-        // entries (4 B), and 4 B of rank per slot whose rank it changed (all on
-        // the first split; bounded by the slots otherwise)
+        // entries (4 B), and 4 B of rank per slot of round 0's split (none on
+        // the initial split; bounded by the slots on later ones)
         if (S->profile && !S->prof_pending.empty() && S->prof_pending.back().name &&
             strncmp(S->prof_pending.back().name, "k_split_apply", 13) == 0)
-            S->prof_pending.back().bytes += 8ll * A + 4ll * (A_prev - A) + (first_split ? 4ll * A_prev : 0);
-        first_split = false;
+            S->prof_pending.back().bytes += 8ll * A + 4ll * (A_prev - A) + (last_mode == kRankAll ? 4ll * A_prev : 0);
         if (A == 0) break;
         if (debug_on())
             debug_log("round %d: active %d medium %d/%d tile %d/%d large %d/%d", round, A, hcnt[CNT_MED],
@@ -973,6 +1002,7 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
         QZ_LAUNCH(S, st, "k_gather_small", 16ll * A + 4ll * small_el,
                   k_gather_small<<<grid_for((A + 31) / 32, kWarps, S->sms * 16), kThreads, 0, st>>>(
                       S->counters + act, f.G[cur], f.key, f.W[cur], ga));
+        if (round == 0) rank_fixup(N - A);
         QZ_LAUNCH(S, st, "k_sort_straddle", 4ll * A,
                   k_sort_straddle<<<grid_for((A + 31) / 32, kWarps, S->sms * 16), kThreads, 0, st>>>(
                       S->counters + act, f.G[cur], f.key, f.W[cur]));
@@ -981,11 +1011,13 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
             dump_array("rsorted_key", f.key, 4 * (size_t)A, st);
             dump_array("rsorted_W", f.W[cur], 4 * (size_t)A, st);
         }
-        split(A, false);
+        last_mode = round == 0 ? kRankAll : kRankChanged;
+        split(A, last_mode);
         dump_split();
         A_prev = A;
         ++round;
     }
+    if (!fixed_up) rank_fixup(N);  // the initial sort finished every suffix
 
     // ---- U and primary indexes: SA read, one byte gathered, one written
     QZ_LAUNCH(S, st, "k_extract", 6 * N,
