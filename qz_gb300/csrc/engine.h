@@ -20,7 +20,7 @@ namespace qz {
 
 // Segment classes of the per-round sort (by group length).
 constexpr int kSmallMax = 16;    // one thread, register bitonic network
-constexpr int kMedMax = 512;     // one warp, register bitonic sort across lanes
+constexpr int kMedMax = 512;     // one warp sorts a group of up to kMedMax slots
 constexpr int kOT = 4096;        // one CTA sorts a group of up to kOT slots; longer: onesweep tiles
 constexpr int kInitTile = 4096;  // text positions per tile of the per-block passes
 constexpr int kMaxRounds = 40;   // prefix doubling needs <= 31 rounds for n < 2^31

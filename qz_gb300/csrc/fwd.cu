@@ -365,18 +365,105 @@ __global__ void __launch_bounds__(kThreads) k_sort_straddle(const int* __restric
     }
 }
 
+// 65..512 slots: stable LSD radix sort by one warp in its share of shared
+// memory (key / suffix ping-pong buffers and 256 digit counters); lane l
+// holds slots it*32 + l, ranks within equal digits come from warp matches;
+// 8-bit digits that are equal across the whole group are skipped.
+constexpr size_t kMedWarpSmem = (size_t)kMedMax * 16 + 256 * 4;
+
+__device__ __forceinline__ void warp_radix_sort(uint32_t* __restrict__ key, int* __restrict__ W, int s, int len,
+                                                unsigned char* wsm) {
+    uint32_t* ks = reinterpret_cast<uint32_t*>(wsm);
+    uint32_t* kd = ks + kMedMax;
+    int* vs = reinterpret_cast<int*>(kd + kMedMax);
+    int* vd = vs + kMedMax;
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(vd + kMedMax);
+    const int ln = (int)lane_id();
+    const unsigned lt = (1u << ln) - 1u;
+    uint32_t kor = 0, kand = 0xffffffffu;
+    for (int j = ln; j < len; j += 32) {
+        uint32_t k = key[s + j];
+        ks[j] = k;
+        vs[j] = W[s + j];
+        kor |= k;
+        kand &= k;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        kor |= __shfl_xor_sync(0xffffffffu, kor, d);
+        kand &= __shfl_xor_sync(0xffffffffu, kand, d);
+    }
+    const uint32_t diff = kor ^ kand;
+    const int nit = (len + 31) >> 5;
+    __syncwarp();
+    for (int pass = 0; pass < 4; ++pass) {
+        const int sh = 8 * pass;
+        if (((diff >> sh) & 255u) == 0) continue;
+        reinterpret_cast<uint4*>(cnt)[2 * ln] = make_uint4(0, 0, 0, 0);
+        reinterpret_cast<uint4*>(cnt)[2 * ln + 1] = make_uint4(0, 0, 0, 0);
+        __syncwarp();
+        uint32_t rk[kMedMax / 32];
+#pragma unroll
+        for (int it = 0; it < kMedMax / 32; ++it) {
+            if (it < nit) {
+                const int i = it * 32 + ln;
+                const bool valid = i < len;
+                const unsigned dg = valid ? (ks[i] >> sh) & 255u : 256u;
+                const unsigned peers = __match_any_sync(0xffffffffu, dg);
+                const unsigned before = __popc(peers & lt);
+                const uint32_t prev = valid ? cnt[dg] : 0u;
+                __syncwarp();
+                if (valid && before == 0) cnt[dg] = prev + __popc(peers);
+                __syncwarp();
+                rk[it] = prev + before;
+            }
+        }
+        {
+            // exclusive scan of the counters, eight consecutive digits per lane
+            uint4 a = reinterpret_cast<uint4*>(cnt)[2 * ln], b = reinterpret_cast<uint4*>(cnt)[2 * ln + 1];
+            uint32_t t0 = a.x, t1 = t0 + a.y, t2 = t1 + a.z, t3 = t2 + a.w;
+            uint32_t t4 = t3 + b.x, t5 = t4 + b.y, t6 = t5 + b.z, t7 = t6 + b.w;
+            uint32_t ex = warp_incl_sum(t7) - t7;
+            reinterpret_cast<uint4*>(cnt)[2 * ln] = make_uint4(ex, ex + t0, ex + t1, ex + t2);
+            reinterpret_cast<uint4*>(cnt)[2 * ln + 1] = make_uint4(ex + t3, ex + t4, ex + t5, ex + t6);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int it = 0; it < kMedMax / 32; ++it) {
+            const int i = it * 32 + ln;
+            if (it < nit && i < len) {
+                const uint32_t k = ks[i];
+                const uint32_t p = cnt[(k >> sh) & 255u] + rk[it];
+                kd[p] = k;
+                vd[p] = vs[i];
+            }
+        }
+        __syncwarp();
+        uint32_t* tk = ks;
+        ks = kd;
+        kd = tk;
+        int* tv = vs;
+        vs = vd;
+        vd = tv;
+    }
+    for (int j = ln; j < len; j += 32) {
+        key[s + j] = ks[j];
+        W[s + j] = vs[j];
+    }
+    __syncwarp();
+}
+
 // Groups of 17..512 slots, one warp per listed group.  Up to 64 slots: two
 // slots per lane, each ranks itself by counting smaller keys (ties by slot)
-// over shuffled keys.  65..512 slots: a bitonic sort in the warp's share of
-// shared memory (loops, not unrolled, so the kernel stays small).
+// over shuffled keys.  65..512 slots: warp_radix_sort.
 __global__ void __launch_bounds__(kThreads) k_sort_medium(const int2* __restrict__ list,
                                                           const int* __restrict__ d_count,
                                                           uint32_t* __restrict__ key, int* __restrict__ W) {
-    __shared__ unsigned long long buf[kWarps][kMedMax];
+    extern __shared__ __align__(16) unsigned char msm[];
     int cnt = *d_count;
     const int nwarps = gridDim.x * kWarps;
     const int ln = (int)lane_id();
-    unsigned long long* sb = buf[warp_id()];
+    unsigned char* wsm = msm + warp_id() * kMedWarpSmem;
     for (int i = blockIdx.x * kWarps + (int)warp_id(); i < cnt; i += nwarps) {
         int2 d = list[i];
         const int s = d.x, len = d.y;
@@ -400,31 +487,7 @@ __global__ void __launch_bounds__(kThreads) k_sort_medium(const int2* __restrict
             }
             continue;
         }
-        int np = 128;
-        while (np < len) np <<= 1;
-        for (int j = ln; j < np; j += 32) sb[j] = j < len ? pack_kv(key[s + j], W[s + j]) : ~0ull;
-        __syncwarp();
-        for (int k = 2; k <= np; k <<= 1) {
-            for (int jj = k >> 1; jj > 0; jj >>= 1) {
-                for (int a = ln; a < np; a += 32) {
-                    int l = a ^ jj;
-                    if (l > a) {
-                        unsigned long long x = sb[a], y = sb[l];
-                        bool up = (a & k) == 0;
-                        if (up ? (x > y) : (x < y)) {
-                            sb[a] = y;
-                            sb[l] = x;
-                        }
-                    }
-                }
-                __syncwarp();
-            }
-        }
-        for (int j = ln; j < len; j += 32) {
-            key[s + j] = (uint32_t)(sb[j] >> 32);
-            W[s + j] = (int)(uint32_t)sb[j];
-        }
-        __syncwarp();
+        warp_radix_sort(key, W, s, len, wsm);
     }
 }
 
@@ -786,10 +849,17 @@ void sort_groups(Storage* S, const int* hc, int A, const int* d_A, uint32_t* key
     if (small_el > 0 && !small_done)
         QZ_LAUNCH(S, st, "k_sort_small", 4ll * A + 16ll * small_el,
                   k_sort_small<<<grid_for(A, kThreads, sms * 16), kThreads, 0, st>>>(d_A, G, key, W));
-    if (nmd > 0)
+    if (nmd > 0) {
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(k_sort_medium, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(kWarps * kMedWarpSmem));
+            attr = true;
+        }
         QZ_LAUNCH(S, st, "k_sort_medium", 16ll * hc[CNT_MED_ELEMS] + 8ll * nmd,
-                  k_sort_medium<<<grid_for(nmd, kWarps, sms * 16), kThreads, 0, st>>>(f.list_med, cnt + CNT_MED,
-                                                                                      key, W));
+                  k_sort_medium<<<grid_for(nmd, kWarps, sms * 16), kThreads, kWarps * kMedWarpSmem, st>>>(
+                      f.list_med, cnt + CNT_MED, key, W));
+    }
     sort_tile_groups(S, f.list_tile, cnt + CNT_TILE, hc[CNT_TILE], hc[CNT_TILE_ELEMS], key, W, st);
     sort_big_groups(S, f.list_large, cnt + CNT_LARGE, nlg, hc[CNT_LARGE_ELEMS], key, W, st);
 }

@@ -28,8 +28,10 @@ constexpr unsigned kSpinLimit = 1u << 24;
 
 // ------------------------------------------------------------------ one-tile groups
 
-// One CTA per group of kTileMin..kOT slots: four stable 8-bit passes in
-// shared memory (warp match-based ranks; ping-pong key/value buffers).
+// One CTA per group of kTileMin..kOT slots: stable 8-bit passes in shared
+// memory (warp match-based ranks; ping-pong key/value buffers).  Each warp
+// takes an equal contiguous share of the group (a multiple of 32 slots), and
+// digits that are equal across the whole group are skipped.
 __global__ void __launch_bounds__(kThreads) k_tile_sort(const int2* __restrict__ list, const int* __restrict__ d_count,
                                                         uint32_t* __restrict__ key, int* __restrict__ val) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -40,38 +42,66 @@ __global__ void __launch_bounds__(kThreads) k_tile_sort(const int2* __restrict__
     uint32_t(*wcnt)[256] = reinterpret_cast<uint32_t(*)[256]>(v1 + kOT);
     __shared__ uint32_t dig_off[256];
     __shared__ uint32_t sh[kWarps + 1];
+    __shared__ uint32_t s_or[kWarps], s_and[kWarps];
     const unsigned w = warp_id(), ln = lane_id();
     const unsigned lt_mask = (1u << ln) - 1u;
     int cnt = *d_count;
     for (int g = blockIdx.x; g < cnt; g += gridDim.x) {
         int2 d = list[g];
         int s = d.x, len = d.y;
+        uint32_t kor = 0, kand = 0xffffffffu;
         for (int i = threadIdx.x; i < len; i += kThreads) {
-            k0[i] = key[s + i];
+            uint32_t k = key[s + i];
+            k0[i] = k;
             v0[i] = val[s + i];
+            kor |= k;
+            kand &= k;
         }
+#pragma unroll
+        for (int dd = 16; dd > 0; dd >>= 1) {
+            kor |= __shfl_xor_sync(0xffffffffu, kor, dd);
+            kand &= __shfl_xor_sync(0xffffffffu, kand, dd);
+        }
+        if (ln == 0) {
+            s_or[w] = kor;
+            s_and[w] = kand;
+        }
+        __syncthreads();
+        kor = 0;
+        kand = 0xffffffffu;
+#pragma unroll
+        for (int q = 0; q < kWarps; ++q) {
+            kor |= s_or[q];
+            kand &= s_and[q];
+        }
+        const uint32_t diff = kor ^ kand;
+        const int nit = (len + kThreads - 1) / kThreads;  // slots per lane
+        const int span = nit * 32;                         // slots per warp
         uint32_t* ks = k0;
         int* vs = v0;
         uint32_t* kd = k1;
         int* vd = v1;
         for (int pass = 0; pass < 4; ++pass) {
             const int shift = 8 * pass;
+            if (((diff >> shift) & 255u) == 0) continue;
 #pragma unroll
             for (int q = 0; q < kWarps; ++q) wcnt[q][threadIdx.x] = 0;
             __syncthreads();
             uint32_t rk[kOItems];
 #pragma unroll
             for (int it = 0; it < kOItems; ++it) {
-                int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
-                bool valid = i < len;
-                unsigned dg = valid ? (ks[i] >> shift) & 255u : 256u;
-                unsigned peers = __match_any_sync(0xffffffffu, dg);
-                unsigned before = __popc(peers & lt_mask);
-                uint32_t prev = valid ? wcnt[w][dg] : 0u;
-                __syncwarp();
-                if (valid && before == 0) wcnt[w][dg] = prev + __popc(peers);
-                __syncwarp();
-                rk[it] = prev + before;
+                if (it < nit) {
+                    int i = (int)w * span + it * 32 + (int)ln;
+                    bool valid = i < len;
+                    unsigned dg = valid ? (ks[i] >> shift) & 255u : 256u;
+                    unsigned peers = __match_any_sync(0xffffffffu, dg);
+                    unsigned before = __popc(peers & lt_mask);
+                    uint32_t prev = valid ? wcnt[w][dg] : 0u;
+                    __syncwarp();
+                    if (valid && before == 0) wcnt[w][dg] = prev + __popc(peers);
+                    __syncwarp();
+                    rk[it] = prev + before;
+                }
             }
             __syncthreads();
             {
@@ -89,8 +119,8 @@ __global__ void __launch_bounds__(kThreads) k_tile_sort(const int2* __restrict__
             __syncthreads();
 #pragma unroll
             for (int it = 0; it < kOItems; ++it) {
-                int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
-                if (i < len) {
+                int i = (int)w * span + it * 32 + (int)ln;
+                if (it < nit && i < len) {
                     uint32_t kv = ks[i];
                     unsigned dg = (kv >> shift) & 255u;
                     uint32_t p = dig_off[dg] + wcnt[w][dg] + rk[it];
