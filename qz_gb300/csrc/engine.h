@@ -53,6 +53,7 @@ struct FwdBuffers {
     int2* list_med;    // groups of 17..512 slots
     int2* list_tile;   // groups of 513..4096 slots
     int2* list_large;  // groups of more than 4096 slots
+    uint8_t* straddle;  // per 32-slot window: a small group may cross its right boundary
     uint32_t* h4;      // large groups: digit counts of all four passes
     unsigned long long* status64;  // look-back status per (tile, digit)
     uint32_t* ltc;     // large: tiles per group -> tile base

@@ -273,66 +273,122 @@ __global__ void __launch_bounds__(kThreads) k_sort_small(const int* __restrict__
 }
 
 // Doubling rounds: secondary keys of all active slots, with groups of 2..16
-// slots that lie inside a 32-slot warp window sorted on the spot.  Each lane
-// gathers the key of its slot; group bounds come from ballots over G; a lane
-// of an in-window small group takes its rank in the group by counting smaller
-// keys (ties by slot) and writes key and suffix there.  Every other slot keeps
-// its suffix and gets its key written in place (sorted later by its class).
+// slots sorted on the spot.  Each warp takes a run of kGatherRun consecutive
+// 32-slot windows.  Each lane gathers the key of its slot; group bounds come
+// from ballots over G; a lane of an in-window small group takes its rank in
+// the group by counting smaller keys (ties by slot) and writes key and suffix
+// there.  Every other slot gets its key written in place (sorted later by its
+// class).  A small group that crosses the boundary between two windows of the
+// run is then re-ranked from the registers of both windows (it lies in the
+// 32-slot window centred on the boundary); boundaries between runs are
+// flagged for k_sort_straddle.
+constexpr int kGatherRun = 8;
+
+__device__ __forceinline__ void rank_centred(uint32_t ck, int cx, int cs, int L, int cbase, uint32_t* __restrict__ key,
+                                             int* __restrict__ W) {
+    const int ln = (int)lane_id();
+    const bool m = ln >= cs && ln < cs + L;
+    int r = 0;
+    for (int j = 0; j < L; ++j) {
+        uint32_t kj = __shfl_sync(0xffffffffu, ck, cs + j);
+        if (m) r += (kj < ck || (kj == ck && cs + j < ln)) ? 1 : 0;
+    }
+    if (m) {
+        key[cbase + cs + r] = ck;
+        W[cbase + cs + r] = cx;
+    }
+}
+
 __global__ void __launch_bounds__(kThreads) k_gather_small(const int* __restrict__ d_A, const int* __restrict__ G,
                                                            uint32_t* __restrict__ key, int* __restrict__ W,
-                                                           GatherArgs ga) {
+                                                           GatherArgs ga, uint8_t* __restrict__ straddle) {
     const int A = *d_A;
     const int ln = (int)lane_id();
     const int nwin = (A + 31) / 32;
+    const int nruns = (nwin + kGatherRun - 1) / kGatherRun;
     const int nwarps = gridDim.x * kWarps;
-    for (int win = blockIdx.x * kWarps + (int)warp_id(); win < nwin; win += nwarps) {
-        const int base = win * 32;
-        const int k = base + ln;
-        const bool valid = k < A;
-        int g = valid ? G[k] : -1;
-        int x = valid ? W[k] : 0;
-        int gp = __shfl_up_sync(0xffffffffu, g, 1);
-        if (ln == 0) gp = (base > 0) ? G[base - 1] : -2;
-        int gn = __shfl_down_sync(0xffffffffu, g, 1);
-        if (ln == 31) gn = (k + 1 < A) ? G[k + 1] : -2;
-        uint32_t kv = 0;
-        if (valid) kv = rank_key(ga, block_span(ga, x), x);
-        const unsigned H = __ballot_sync(0xffffffffu, valid && gp != g);
-        const unsigned T = __ballot_sync(0xffffffffu, valid && (k + 1 >= A || gn != g));
-        const unsigned hb = H & (0xffffffffu >> (31 - ln));
-        const unsigned tb = T & (0xffffffffu << ln);
-        const int s = hb ? 31 - __clz(hb) : -1;
-        const int e = tb ? __ffs(tb) - 1 : 32;
-        const bool inside = valid && s >= 0 && e < 32;
-        const int L = inside ? e - s + 1 : 0;
-        const bool mine = inside && L >= 2 && L <= kSmallMax;
-        int maxL = mine ? L : 0;
+    for (int run = blockIdx.x * kWarps + (int)warp_id(); run < nruns; run += nwarps) {
+        const int w_begin = run * kGatherRun, w_end = min(nwin, w_begin + kGatherRun);
+        uint32_t pkv = 0;
+        int px = 0, ps = 32;
+        bool ptail = false;
+        for (int win = w_begin; win < w_end; ++win) {
+            const int base = win * 32;
+            const int k = base + ln;
+            const bool valid = k < A;
+            int g = valid ? G[k] : -1;
+            int x = valid ? W[k] : 0;
+            int gp = __shfl_up_sync(0xffffffffu, g, 1);
+            if (ln == 0) gp = (base > 0) ? G[base - 1] : -2;
+            int gn = __shfl_down_sync(0xffffffffu, g, 1);
+            if (ln == 31) gn = (k + 1 < A) ? G[k + 1] : -2;
+            uint32_t kv = 0;
+            if (valid) kv = rank_key(ga, block_span(ga, x), x);
+            const unsigned H = __ballot_sync(0xffffffffu, valid && gp != g);
+            const unsigned T = __ballot_sync(0xffffffffu, valid && (k + 1 >= A || gn != g));
+            const unsigned hb = H & (0xffffffffu >> (31 - ln));
+            const unsigned tb = T & (0xffffffffu << ln);
+            const int s = hb ? 31 - __clz(hb) : -1;
+            const int e = tb ? __ffs(tb) - 1 : 32;
+            const bool inside = valid && s >= 0 && e < 32;
+            const int L = inside ? e - s + 1 : 0;
+            const bool mine = inside && L >= 2 && L <= kSmallMax;
+            int maxL = mine ? L : 0;
 #pragma unroll
-        for (int d = 16; d > 0; d >>= 1) maxL = max(maxL, __shfl_xor_sync(0xffffffffu, maxL, d));
-        int rank = 0;
-        for (int j = 0; j < maxL; ++j) {
-            int src = (mine ? s : 0) + j;
-            uint32_t kj = __shfl_sync(0xffffffffu, kv, src & 31);
-            if (mine && j < L) rank += (kj < kv || (kj == kv && src < ln)) ? 1 : 0;
-        }
-        if (mine) {
-            __stcs(key + base + s + rank, kv);
-            __stcs(W + base + s + rank, x);
-        } else if (valid) {
-            __stcs(key + k, kv);
+            for (int d = 16; d > 0; d >>= 1) maxL = max(maxL, __shfl_xor_sync(0xffffffffu, maxL, d));
+            int rank = 0;
+            for (int j = 0; j < maxL; ++j) {
+                int src = (mine ? s : 0) + j;
+                uint32_t kj = __shfl_sync(0xffffffffu, kv, src & 31);
+                if (mine && j < L) rank += (kj < kv || (kj == kv && src < ln)) ? 1 : 0;
+            }
+            if (mine) {
+                __stcs(key + base + s + rank, kv);
+                __stcs(W + base + s + rank, x);
+            } else if (valid) {
+                __stcs(key + k, kv);
+            }
+            // the previous window's last group continues here: if it is small
+            // it lies in the centred window (previous lanes 16..31, these 0..15)
+            if (ptail) {
+                const int e0 = T ? __ffs(T) - 1 : 32;
+                const int Lc = (32 - ps) + e0 + 1;
+                if (e0 < 16 && Lc <= kSmallMax) {
+                    __syncwarp();
+                    const uint32_t a = __shfl_sync(0xffffffffu, pkv, (ln + 16) & 31);
+                    const uint32_t b = __shfl_sync(0xffffffffu, kv, (ln + 16) & 31);
+                    const int ax = __shfl_sync(0xffffffffu, px, (ln + 16) & 31);
+                    const int bx = __shfl_sync(0xffffffffu, x, (ln + 16) & 31);
+                    rank_centred(ln < 16 ? a : b, ln < 16 ? ax : bx, ps - 16, Lc, base - 16, key, W);
+                }
+            }
+            // this window's last group runs on and started in its upper half
+            const bool tail = __shfl_sync(0xffffffffu, valid && gn == g && s >= 16, 31);
+            ps = __shfl_sync(0xffffffffu, s, 31);
+            ptail = tail;
+            pkv = kv;
+            px = x;
+            if (win == w_end - 1) {
+                if (ln == 0) straddle[run] = tail ? 1 : 0;
+            }
         }
     }
 }
 
-// Groups of 2..16 slots that cross a multiple of 32: each lies inside the
-// 32-slot window centred on that boundary, where it is ranked as above.
+// Groups of 2..16 slots that cross the boundary after the last window of a
+// gather run: each lies inside the 32-slot window centred on that boundary,
+// where it is ranked as above.  Only flagged boundaries are visited.
 __global__ void __launch_bounds__(kThreads) k_sort_straddle(const int* __restrict__ d_A, const int* __restrict__ G,
-                                                            uint32_t* __restrict__ key, int* __restrict__ W) {
+                                                            uint32_t* __restrict__ key, int* __restrict__ W,
+                                                            const uint8_t* __restrict__ straddle) {
     const int A = *d_A;
     const int ln = (int)lane_id();
-    const int nwin = (A + 31) / 32;  // boundaries at 32, 64, ...
+    const int nwin = (A + 31) / 32;
+    const int nruns = (nwin + kGatherRun - 1) / kGatherRun;
     const int nwarps = gridDim.x * kWarps;
-    for (int win = blockIdx.x * kWarps + (int)warp_id(); win + 1 < nwin; win += nwarps) {
+    for (int run = blockIdx.x * kWarps + (int)warp_id(); run < nruns; run += nwarps) {
+        if (!straddle[run]) continue;  // uniform across the warp
+        const int win = min(nwin, (run + 1) * kGatherRun) - 1;
         const int base = win * 32 + 16;
         const int k = base + ln;
         const bool valid = k < A;
@@ -353,15 +409,7 @@ __global__ void __launch_bounds__(kThreads) k_sort_straddle(const int* __restric
         const bool mine = ln >= s && ln <= e;
         uint32_t kv = mine ? key[k] : 0u;
         int wv = mine ? W[k] : 0;
-        int rank = 0;
-        for (int j = 0; j < L; ++j) {
-            uint32_t kj = __shfl_sync(0xffffffffu, kv, s + j);
-            if (mine) rank += (kj < kv || (kj == kv && s + j < ln)) ? 1 : 0;
-        }
-        if (mine) {
-            key[base + s + rank] = kv;
-            W[base + s + rank] = wv;
-        }
+        rank_centred(kv, wv, s, L, base, key, W);
     }
 }
 
@@ -1070,12 +1118,16 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
         // groups inside a warp window sorted on the spot (suffix rewritten)
         long long small_el = (long long)A - hcnt[CNT_MED_ELEMS] - hcnt[CNT_TILE_ELEMS] - hcnt[CNT_LARGE_ELEMS];
         QZ_LAUNCH(S, st, "k_gather_small", 16ll * A + 4ll * small_el,
-                  k_gather_small<<<grid_for((A + 31) / 32, kWarps, S->sms * 16), kThreads, 0, st>>>(
-                      S->counters + act, f.G[cur], f.key, f.W[cur], ga));
+                  k_gather_small<<<grid_for(((A + 31) / 32 + kGatherRun - 1) / kGatherRun, kWarps, S->sms * 16),
+                                   kThreads, 0, st>>>(
+                      S->counters + act, f.G[cur], f.key, f.W[cur], ga, f.straddle));
         if (round == 0) rank_fixup(N - A);
-        QZ_LAUNCH(S, st, "k_sort_straddle", 4ll * A,
-                  k_sort_straddle<<<grid_for((A + 31) / 32, kWarps, S->sms * 16), kThreads, 0, st>>>(
-                      S->counters + act, f.G[cur], f.key, f.W[cur]));
+        // one flag byte per gather run; flagged runs: group ranks of one window,
+        // keys and suffixes of the straddling group
+        const long long nruns = ((A + 31) / 32 + kGatherRun - 1) / kGatherRun;
+        QZ_LAUNCH(S, st, "k_sort_straddle", nruns,
+                  k_sort_straddle<<<grid_for(nruns, kWarps, S->sms * 16), kThreads, 0, st>>>(
+                      S->counters + act, f.G[cur], f.key, f.W[cur], f.straddle));
         sort_groups(S, hcnt, A, S->counters + act, f.key, f.W[cur], f.G[cur], st, true);
         if (dump) {
             dump_array("rsorted_key", f.key, 4 * (size_t)A, st);

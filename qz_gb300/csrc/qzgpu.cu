@@ -185,6 +185,7 @@ size_t layout(Storage* S, char* base, const Caps& c) {
         f.wsv[i] = cv.take<int>(c.N);
     }
     f.list_med = cv.take<int2>(c.med);
+    f.straddle = cv.take<uint8_t>(c.N / 32 + 64);
     f.list_tile = cv.take<int2>(c.tile);
     f.list_large = cv.take<int2>(c.large);
     f.h4 = cv.take<uint32_t>(1024 * c.large);
