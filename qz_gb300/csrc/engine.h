@@ -38,6 +38,8 @@ enum Counter {
     CNT_TILE = 10,
     CNT_TILE_ELEMS = 11,
     CNT_TICKET = 12,    // tile tickets of a look-back radix pass
+    CNT_PAIR = 13,      // groups of 17..64 slots (rank-by-count class)
+    CNT_PAIR_ELEMS = 14,
     CNT_LARGE_ELEMS = 9,
     CNT_SLOTS = 16,
 };
@@ -50,7 +52,8 @@ struct FwdBuffers {
     int* G[2];   // compact slots: group rank (SA position of the group's first slot)
     uint32_t* wsk[2];
     int* wsv[2];
-    int2* list_med;    // groups of 17..512 slots
+    int2* list_rbc;    // groups of 17..64 slots (rank by count)
+    int2* list_med;    // groups of 65..medium_max slots (warp radix)
     int2* list_tile;   // groups of 513..4096 slots
     int2* list_large;  // groups of more than 4096 slots
     uint8_t* straddle;  // per 32-slot window: a small group may cross its right boundary

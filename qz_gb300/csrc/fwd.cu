@@ -501,41 +501,63 @@ __device__ __forceinline__ void warp_radix_sort(uint32_t* __restrict__ key, int*
     __syncwarp();
 }
 
-// Groups of 17..512 slots, one warp per listed group.  Up to 64 slots: two
-// slots per lane, each ranks itself by counting smaller keys (ties by slot)
-// over shuffled keys.  65..512 slots: warp_radix_sort.
+// Groups of 17..64 slots, one warp per listed group: each slot ranks itself by
+// counting smaller keys (ties by slot) over shuffled keys; one slot per lane
+// up to 32 slots, two above.
+__global__ void __launch_bounds__(kThreads) k_sort_rbc(const int2* __restrict__ list, const int* __restrict__ d_count,
+                                                       uint32_t* __restrict__ key, int* __restrict__ W) {
+    int cnt = *d_count;
+    const int nwarps = gridDim.x * kWarps;
+    const int ln = (int)lane_id();
+    for (int i = blockIdx.x * kWarps + (int)warp_id(); i < cnt; i += nwarps) {
+        int2 d = list[i];
+        const int s = d.x, len = d.y;
+        bool v0 = ln < len;
+        uint32_t k0 = v0 ? key[s + ln] : 0xffffffffu;
+        int w0 = v0 ? W[s + ln] : 0;
+        int r0 = 0;
+        if (len <= 32) {
+            for (int j = 0; j < len; ++j) {
+                uint32_t kj = __shfl_sync(0xffffffffu, k0, j);
+                r0 += (kj < k0 || (kj == k0 && j < ln)) ? 1 : 0;
+            }
+            if (v0) {
+                key[s + r0] = k0;
+                W[s + r0] = w0;
+            }
+            continue;
+        }
+        bool v1 = ln + 32 < len;
+        uint32_t k1 = v1 ? key[s + ln + 32] : 0xffffffffu;
+        int w1 = v1 ? W[s + ln + 32] : 0;
+        int r1 = 0;
+        for (int j = 0; j < len; ++j) {
+            uint32_t kj = __shfl_sync(0xffffffffu, j < 32 ? k0 : k1, j & 31);
+            r0 += (kj < k0 || (kj == k0 && j < ln)) ? 1 : 0;
+            r1 += (kj < k1 || (kj == k1 && j < ln + 32)) ? 1 : 0;
+        }
+        if (v0) {
+            key[s + r0] = k0;
+            W[s + r0] = w0;
+        }
+        if (v1) {
+            key[s + r1] = k1;
+            W[s + r1] = w1;
+        }
+    }
+}
+
+// Groups of 65..512 slots, one warp per listed group: warp_radix_sort.
 __global__ void __launch_bounds__(kThreads) k_sort_medium(const int2* __restrict__ list,
                                                           const int* __restrict__ d_count,
                                                           uint32_t* __restrict__ key, int* __restrict__ W) {
     extern __shared__ __align__(16) unsigned char msm[];
     int cnt = *d_count;
     const int nwarps = gridDim.x * kWarps;
-    const int ln = (int)lane_id();
     unsigned char* wsm = msm + warp_id() * kMedWarpSmem;
     for (int i = blockIdx.x * kWarps + (int)warp_id(); i < cnt; i += nwarps) {
         int2 d = list[i];
-        const int s = d.x, len = d.y;
-        if (len <= 64) {
-            bool v0 = ln < len, v1 = ln + 32 < len;
-            uint32_t k0 = v0 ? key[s + ln] : 0xffffffffu, k1 = v1 ? key[s + ln + 32] : 0xffffffffu;
-            int w0 = v0 ? W[s + ln] : 0, w1 = v1 ? W[s + ln + 32] : 0;
-            int r0 = 0, r1 = 0;
-            for (int j = 0; j < len; ++j) {
-                uint32_t kj = __shfl_sync(0xffffffffu, j < 32 ? k0 : k1, j & 31);
-                r0 += (kj < k0 || (kj == k0 && j < ln)) ? 1 : 0;
-                r1 += (kj < k1 || (kj == k1 && j < ln + 32)) ? 1 : 0;
-            }
-            if (v0) {
-                key[s + r0] = k0;
-                W[s + r0] = w0;
-            }
-            if (v1) {
-                key[s + r1] = k1;
-                W[s + r1] = w1;
-            }
-            continue;
-        }
-        warp_radix_sort(key, W, s, len, wsm);
+        warp_radix_sort(key, W, d.x, d.y, wsm);
     }
 }
 
@@ -570,6 +592,7 @@ struct SplitArgs {
     int* SA;
     int* Wn;
     int* Gn;
+    int2* list_rbc;
     int2* list_med;
     int2* list_tile;
     int2* list_large;
@@ -735,6 +758,8 @@ __global__ void __launch_bounds__(kThreads) k_pscan_top(SplitArgs a, uint32_t* _
     if (threadIdx.x == 0) {
         *a.A_next = (int)carry;
         a.counters[CNT_MED] = 0;
+        a.counters[CNT_PAIR] = 0;
+        a.counters[CNT_PAIR_ELEMS] = 0;
         a.counters[CNT_TILE] = 0;
         a.counters[CNT_LARGE] = 0;
         a.counters[CNT_MED_ELEMS] = 0;
@@ -810,23 +835,21 @@ __global__ void __launch_bounds__(kThreads, 5) k_split_apply(SplitArgs a) {
                 } else {
                     __stcs(a.Wn + d, w);
                     __stcs(a.Gn + d, rank);
-                    if (t.nsh[i]) {
-                        int L = kk - ks + 1;
-                        if (L > kSmallMax) {
-                            int2 dsc = make_int2((int)d - L + 1, L);
-                            if (L <= a.medium_max) {
-                                a.list_med[atomicAdd(&a.counters[CNT_MED], 1)] = dsc;
-                                atomicAdd(&a.counters[CNT_MED_ELEMS], L);
-                            } else if (L <= kOT) {
-                                a.list_tile[atomicAdd(&a.counters[CNT_TILE], 1)] = dsc;
-                                atomicAdd(&a.counters[CNT_TILE_ELEMS], L);
-                            } else {
-                                a.list_large[atomicAdd(&a.counters[CNT_LARGE], 1)] = dsc;
-                                atomicAdd(&a.counters[CNT_LARGE_ELEMS], L);
-                            }
-                        }
-                    }
                 }
+            }
+            // a surviving subgroup ends here: list it by class (one atomic per
+            // class and warp step for the descriptors, one for the slot count)
+            const int L = kk - ks + 1;
+            const bool ends = surv && t.nsh[i] && L > kSmallMax;
+            const int cls = !ends ? -1 : (L <= 64 ? 3 : (L <= a.medium_max ? 0 : (L <= kOT ? 1 : 2)));
+            const int2 dsc = make_int2((int)d - L + 1, L);
+            if (ends) {
+                const int ci = cls == 0 ? CNT_MED : (cls == 1 ? CNT_TILE : (cls == 2 ? CNT_LARGE : CNT_PAIR));
+                const int ce = cls == 0 ? CNT_MED_ELEMS
+                                        : (cls == 1 ? CNT_TILE_ELEMS : (cls == 2 ? CNT_LARGE_ELEMS : CNT_PAIR_ELEMS));
+                int2* list = cls == 0 ? a.list_med : (cls == 1 ? a.list_tile : (cls == 2 ? a.list_large : a.list_rbc));
+                list[atomicAdd(&a.counters[ci], 1)] = dsc;
+                atomicAdd(&a.counters[ce], L);
             }
         }
     }
@@ -891,8 +914,13 @@ void sort_groups(Storage* S, const int* hc, int A, const int* d_A, uint32_t* key
     FwdBuffers& f = S->f;
     int* cnt = S->counters;
     const int sms = S->sms;
-    int nmd = hc[CNT_MED], nlg = hc[CNT_LARGE];
-    long long small_el = (long long)A - hc[CNT_MED_ELEMS] - hc[CNT_TILE_ELEMS] - hc[CNT_LARGE_ELEMS];
+    int nmd = hc[CNT_MED], nlg = hc[CNT_LARGE], nrb = hc[CNT_PAIR];
+    long long small_el = (long long)A - hc[CNT_PAIR_ELEMS] - hc[CNT_MED_ELEMS] - hc[CNT_TILE_ELEMS] -
+                         hc[CNT_LARGE_ELEMS];
+    if (nrb > 0)
+        QZ_LAUNCH(S, st, "k_sort_rbc", 16ll * hc[CNT_PAIR_ELEMS] + 8ll * nrb,
+                  k_sort_rbc<<<grid_for(nrb, kWarps, sms * 16), kThreads, 0, st>>>(f.list_rbc, cnt + CNT_PAIR, key,
+                                                                                  W));
     // every slot: group rank read; small groups: key and suffix read and written
     if (small_el > 0 && !small_done)
         QZ_LAUNCH(S, st, "k_sort_small", 4ll * A + 16ll * small_el,
@@ -939,12 +967,15 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
     for (int b = 0; b < nb; ++b)
         for (int s = off[b]; s < off[b + 1]; s += kInitTile) tiles.push_back(make_int2(b, s));
     // initial groups = blocks; blocks of <= kSmallMax bytes need no list
-    std::vector<int2> l1, lt, l2;
+    std::vector<int2> l0, l1, lt, l2;
     int cnt0[CNT_SLOTS] = {0};
     for (int b = 0; b < nb; ++b) {
         if (n[b] <= kSmallMax) continue;
         int2 dsc = make_int2(off[b], n[b]);
-        if (n[b] <= S->tune.medium_max) {
+        if (n[b] <= 64) {
+            l0.push_back(dsc);
+            cnt0[CNT_PAIR_ELEMS] += n[b];
+        } else if (n[b] <= S->tune.medium_max) {
             l1.push_back(dsc);
             cnt0[CNT_MED_ELEMS] += n[b];
         } else if (n[b] <= kOT) {
@@ -963,7 +994,7 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
             if (aux_rate[b] > 0 && n[b] > 0) aux_total += (n[b] - 1) / aux_rate[b];
         }
     }
-    size_t need = sizeof(int) * (nb + 1) + sizeof(int2) * (tiles.size() + l1.size() + lt.size() + l2.size()) +
+    size_t need = sizeof(int) * (nb + 1) + sizeof(int2) * (tiles.size() + l0.size() + l1.size() + lt.size() + l2.size()) +
                   sizeof(int) * CNT_SLOTS + sizeof(int) * 2 * nb + 64 * 8;
     if (need > S->pin_tab_bytes || aux_total > 64 * S->cap_blocks) return QZGPU_BAD_PARAMETER;
     char* p = S->pin_tab;
@@ -975,10 +1006,12 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
     };
     char* h_off = put(off.data(), sizeof(int) * off.size());
     char* h_tiles = put(tiles.data(), sizeof(int2) * tiles.size());
+    char* h_l0 = put(l0.data(), sizeof(int2) * l0.size());
     char* h_l1 = put(l1.data(), sizeof(int2) * l1.size());
     char* h_lt = put(lt.data(), sizeof(int2) * lt.size());
     char* h_l2 = put(l2.data(), sizeof(int2) * l2.size());
     cnt0[CNT_ACTIVE] = (int)N;
+    cnt0[CNT_PAIR] = (int)l0.size();
     cnt0[CNT_MED] = (int)l1.size();
     cnt0[CNT_TILE] = (int)lt.size();
     cnt0[CNT_LARGE] = (int)l2.size();
@@ -991,6 +1024,7 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
     };
     h2d(S->blk_off, h_off, sizeof(int) * off.size());
     h2d(S->tiles, h_tiles, sizeof(int2) * tiles.size());
+    h2d(f.list_rbc, h_l0, sizeof(int2) * l0.size());
     h2d(f.list_med, h_l1, sizeof(int2) * l1.size());
     h2d(f.list_tile, h_lt, sizeof(int2) * lt.size());
     h2d(f.list_large, h_l2, sizeof(int2) * l2.size());
@@ -1044,6 +1078,7 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
         a.SA = f.SA;
         a.Wn = f.W[cur ^ 1];
         a.Gn = f.G[cur ^ 1];
+        a.list_rbc = f.list_rbc;
         a.list_med = f.list_med;
         a.list_tile = f.list_tile;
         a.list_large = f.list_large;
@@ -1106,8 +1141,9 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
             S->prof_pending.back().bytes += 8ll * A + 4ll * (A_prev - A) + (last_mode == kRankAll ? 4ll * A_prev : 0);
         if (A == 0) break;
         if (debug_on())
-            debug_log("round %d: active %d medium %d/%d tile %d/%d large %d/%d", round, A, hcnt[CNT_MED],
-                      hcnt[CNT_MED_ELEMS], hcnt[CNT_TILE], hcnt[CNT_TILE_ELEMS], hcnt[CNT_LARGE], hcnt[CNT_LARGE_ELEMS]);
+            debug_log("round %d: active %d rbc %d/%d medium %d/%d tile %d/%d large %d/%d", round, A, hcnt[CNT_PAIR],
+                      hcnt[CNT_PAIR_ELEMS], hcnt[CNT_MED], hcnt[CNT_MED_ELEMS], hcnt[CNT_TILE], hcnt[CNT_TILE_ELEMS],
+                      hcnt[CNT_LARGE], hcnt[CNT_LARGE_ELEMS]);
         if (round >= kMaxRounds) {
             if (debug_on()) debug_log("no convergence after %d rounds", round);
             return QZGPU_GPU_ERROR;
@@ -1116,7 +1152,8 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
         ga.round = round;
         // suffix and group rank read, one rank gathered, key written; small
         // groups inside a warp window sorted on the spot (suffix rewritten)
-        long long small_el = (long long)A - hcnt[CNT_MED_ELEMS] - hcnt[CNT_TILE_ELEMS] - hcnt[CNT_LARGE_ELEMS];
+        long long small_el = (long long)A - hcnt[CNT_PAIR_ELEMS] - hcnt[CNT_MED_ELEMS] - hcnt[CNT_TILE_ELEMS] -
+                             hcnt[CNT_LARGE_ELEMS];
         QZ_LAUNCH(S, st, "k_gather_small", 16ll * A + 4ll * small_el,
                   k_gather_small<<<grid_for(((A + 31) / 32 + kGatherRun - 1) / kGatherRun, kWarps, S->sms * 16),
                                    kThreads, 0, st>>>(

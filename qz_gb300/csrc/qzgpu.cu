@@ -184,7 +184,8 @@ size_t layout(Storage* S, char* base, const Caps& c) {
         f.wsk[i] = cv.take<uint32_t>(c.N);
         f.wsv[i] = cv.take<int>(c.N);
     }
-    f.list_med = cv.take<int2>(c.med);
+    f.list_rbc = cv.take<int2>(c.med);
+    f.list_med = cv.take<int2>(c.N / 65 + 2);
     f.straddle = cv.take<uint8_t>(c.N / 32 + 64);
     f.list_tile = cv.take<int2>(c.tile);
     f.list_large = cv.take<int2>(c.large);
