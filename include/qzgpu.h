@@ -162,6 +162,9 @@ typedef struct qzgpu_kernel_time {
     long long alg_bytes;    /* summed algorithmic HBM bytes of those launches */
 } qzgpu_kernel_time;
 int qzgpu_storage_profile(qzgpu_storage *storage, int enable);
+/* Restricts that timing to the launches of one kernel (by name; NULL or ""
+ * times every kernel again), so that a long run is timed at little cost. */
+int qzgpu_storage_profile_only(qzgpu_storage *storage, const char *name);
 /* Copies up to `max` records (largest total time first); returns the number
  * of kernels recorded.  reset != 0 clears the records afterwards. */
 int qzgpu_storage_profile_read(qzgpu_storage *storage, qzgpu_kernel_time *out, int max, int reset);

@@ -125,8 +125,10 @@ class Storage:
         n = check(self._lib.qzgpu_storage_round_counts(self._h, buf, 64), "qzgpu_storage_round_counts")
         return [int(buf[i]) for i in range(min(n, 64))]
 
-    def profile(self, enable: bool = True) -> None:
-        """Times every later launch on this storage with CUDA events."""
+    def profile(self, enable: bool = True, only: str | None = None) -> None:
+        """Times every later launch on this storage with CUDA events (only the
+        launches of kernel `only` when it is given)."""
+        check(self._lib.qzgpu_storage_profile_only(self._h, (only or "").encode()), "qzgpu_storage_profile_only")
         check(self._lib.qzgpu_storage_profile(self._h, int(enable)), "qzgpu_storage_profile")
 
     def profile_read(self, reset: bool = True) -> list[dict]:

@@ -147,6 +147,7 @@ struct Storage {
         long long bytes = 0;
     };
     bool profile = false;
+    std::string profile_only;  // when set, only launches of this kernel are timed
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_next = 0;
     std::vector<ProfRec> prof_pending;
@@ -175,6 +176,7 @@ struct Engine {
     int job_gen = 0, job_done = 0;
     bool stop = false;
     bool profile = false;
+    std::string profile_only;  // when set, only launches of this kernel are timed
     long long fwd_sub_bytes = kLaneBytes;  // forward sub-batch size (<= lane_bytes)
     long long inv_sub_bytes = kLaneBytes;  // inverse sub-batch size (<= lane_bytes)
     qzgpu_stats stats{};
@@ -226,13 +228,13 @@ void debug_log(const char* fmt, ...);
 // batches to <dir>/<seq>_<name>.bin for offline inspection.
 bool dump_on();
 void dump_array(const char* name, const void* dptr, size_t bytes, cudaStream_t st);
-cudaEvent_t prof_begin(Storage* S, cudaStream_t st);
+cudaEvent_t prof_begin(Storage* S, cudaStream_t st, const char* name);
 void prof_end(Storage* S, cudaStream_t st, const char* name, long long bytes, cudaEvent_t a);
 void prof_flush(Storage* S);  // after the stream is idle: fold pending records in
 // Launch wrapper: counts the launch, times it when profiling, checks it in debug mode.
 #define QZ_LAUNCH(S, st, name, bytes, ...)                     \
     do {                                                       \
-        cudaEvent_t _qz_a = ::qz::prof_begin(S, st);           \
+        cudaEvent_t _qz_a = ::qz::prof_begin(S, st, name);     \
         __VA_ARGS__;                                           \
         ::qz::prof_end(S, st, name, (long long)(bytes), _qz_a); \
         QZ_DBG(st, name);                                      \

@@ -119,7 +119,10 @@ int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned cha
     std::atomic<int> first_err{0};
     std::vector<std::vector<long long>> lane_rounds(K);
     std::vector<int> lane_maxr(K, 0), lane_launch(K, 0);
-    for (auto& s : E->lanes) s->profile = E->profile;
+    for (auto& s : E->lanes) {
+        s->profile = E->profile;
+        s->profile_only = E->profile_only;
+    }
     auto run_sub = [&](int lane, const Sub& sb) {
         Storage* S = E->lanes[lane].get();
         const int cnt = sb.b1 - sb.b0;

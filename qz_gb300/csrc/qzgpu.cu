@@ -50,8 +50,9 @@ void debug_after(cudaStream_t st, const char* what) {
     if (e != cudaSuccess) debug_log("%s: %s", what, cudaGetErrorString(e));
 }
 
-cudaEvent_t prof_begin(Storage* S, cudaStream_t st) {
+cudaEvent_t prof_begin(Storage* S, cudaStream_t st, const char* name) {
     if (!S->profile) return nullptr;
+    if (!S->profile_only.empty() && S->profile_only != name) return nullptr;
     if (S->ev_next + 2 > S->ev_pool.size()) {
         size_t grow = S->ev_pool.size() ? S->ev_pool.size() : 1024;
         for (size_t i = 0; i < grow; ++i) {
@@ -655,6 +656,13 @@ int qzgpu_storage_profile(qzgpu_storage* storage, int enable) {
     if (!storage) return QZGPU_BAD_PARAMETER;
     std::lock_guard<std::mutex> lk(storage->mu);
     storage->profile = enable != 0;
+    return QZGPU_NO_ERROR;
+}
+
+int qzgpu_storage_profile_only(qzgpu_storage* storage, const char* name) {
+    if (!storage) return QZGPU_BAD_PARAMETER;
+    std::lock_guard<std::mutex> lk(storage->mu);
+    storage->profile_only = name ? name : "";
     return QZGPU_NO_ERROR;
 }
 

@@ -71,6 +71,7 @@ SIGNATURES = {
     "qzgpu_bwt_decode_device": (ctypes.c_int, [_vp, ctypes.c_int, _i32p, _i32p, _vp, _vp, _vp]),
     "qzgpu_storage_last_stats": (ctypes.c_int, [_vp, ctypes.POINTER(Stats)]),
     "qzgpu_storage_profile": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "qzgpu_storage_profile_only": (ctypes.c_int, [_vp, ctypes.c_char_p]),
     "qzgpu_storage_set_param": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_longlong]),
     "qzgpu_storage_get_param": (ctypes.c_longlong, [_vp, ctypes.c_char_p]),
     "qzgpu_bwt_decode_noalloc": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),

@@ -175,3 +175,16 @@ def test_tuned_knobs_keep_results(gpu, oracle, params):
         assert all((x == y).all() for x, y in zip(back, blocks))
         with pytest.raises(native.QzGpuError):
             st.set_param("medium_max", 100)
+
+
+def test_profile_only_times_one_kernel(gpu):
+    blocks = [synth.sample_reads(synth.uniform_genome(20_000, seed=81), 200, seed=82)]
+    with bwt.Storage(len(blocks[0]), 1) as st:
+        st.profile(True, only="k_extract")
+        st.encode_batch(blocks)
+        names = {r["name"] for r in st.profile_read()}
+        assert names == {"k_extract"}
+        st.profile(True)
+        st.encode_batch(blocks)
+        assert len(st.profile_read()) > 3
+        st.profile(False)
