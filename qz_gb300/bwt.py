@@ -26,6 +26,13 @@ def _as_u8(data) -> np.ndarray:
     return np.array(data, dtype=np.uint8, copy=True)
 
 
+def _view_u8(data) -> np.ndarray:
+    """Contiguous uint8 view of a caller's buffer (a copy only when needed)."""
+    if isinstance(data, (bytes, bytearray, memoryview)):
+        return np.frombuffer(data, dtype=np.uint8)
+    return np.ascontiguousarray(data, dtype=np.uint8)
+
+
 def _ptr(a: np.ndarray):
     return a.ctypes.data_as(_u8p)
 
@@ -143,24 +150,40 @@ class Storage:
         outp = (_u8p * max(nb, 1))(*[_ptr(b) for b in outs])
         return inp, outp
 
-    def encode_batch(self, blocks):
+    @staticmethod
+    def _outs(sizes, out):
+        if out is None:
+            return [np.empty(max(int(n), 1), np.uint8) for n in sizes]
+        if len(out) != len(sizes):
+            raise QzGpuError(native.QZGPU_BAD_PARAMETER, "out: one buffer per block")
+        outs = []
+        for n, o in zip(sizes, out):
+            if not (isinstance(o, np.ndarray) and o.dtype == np.uint8 and o.flags.c_contiguous and o.flags.writeable
+                    and len(o) >= n):
+                raise QzGpuError(native.QZGPU_BAD_PARAMETER, "out: writable contiguous uint8 arrays of block size")
+            outs.append(o if n else np.zeros(1, np.uint8))
+        return outs
+
+    def encode_batch(self, blocks, out=None):
         """Forward BWT of many blocks in one batched launch sequence.
-        Returns (list of U, list of primary indexes)."""
-        ins = [_as_u8(b) for b in blocks]
+        Returns (list of U, list of primary indexes).  `out`: optional output
+        arrays, one per block (reused across calls by streaming callers)."""
+        ins = [_view_u8(b) for b in blocks]
         ins = [b if len(b) else np.zeros(1, np.uint8) for b in ins]
         sizes = np.array([len(b) for b in blocks] or [0], dtype=np.int32)
-        outs = [np.empty(max(len(b), 1), np.uint8) for b in ins]
+        outs = self._outs([len(b) for b in blocks], out)
         idx = np.zeros(max(len(blocks), 1), dtype=np.int32)
         inp, outp = self._ptr_arrays(ins, outs)
         check(self._lib.qzgpu_bwt_encode_batch(self._h, len(blocks), inp, outp, sizes.ctypes.data_as(_i32p),
                                                idx.ctypes.data_as(_i32p), 0), "qzgpu_bwt_encode_batch")
         return [o[: s] for o, s in zip(outs, sizes)], [int(i) for i in idx[: len(blocks)]]
 
-    def decode_batch(self, blocks, indexes):
-        ins = [_as_u8(b) for b in blocks]
+    def decode_batch(self, blocks, indexes, out=None):
+        """Inverse BWT of many blocks; `out` as for encode_batch."""
+        ins = [_view_u8(b) for b in blocks]
         ins = [b if len(b) else np.zeros(1, np.uint8) for b in ins]
         sizes = np.array([len(b) for b in blocks] or [0], dtype=np.int32)
-        outs = [np.empty(max(len(b), 1), np.uint8) for b in ins]
+        outs = self._outs([len(b) for b in blocks], out)
         idx = np.array(list(indexes) or [0], dtype=np.int32)
         inp, outp = self._ptr_arrays(ins, outs)
         check(self._lib.qzgpu_bwt_decode_batch(self._h, len(blocks), inp, outp, sizes.ctypes.data_as(_i32p),

@@ -214,10 +214,13 @@ int map_cuda_error(cudaError_t e);
 // Host-buffer batch calls on a storage the caller holds (copies in, runs,
 // copies out, synchronises the storage's stream).
 int check_blocks(int nblocks, const int* n, long long* total);
+// Host-buffer calls.  `before_copy_out`, when given, runs after the device
+// work and before the device-to-host copies (the multi-lane engine waits there
+// until the output pages have been touched).
 int encode_host(Storage* S, int nb, const unsigned char* const* T, unsigned char* const* U, const int* n, int* idx,
-                const int* aux_rate, int* aux_out);
+                const int* aux_rate, int* aux_out, const std::function<void()>* before_copy_out = nullptr);
 int decode_host(Storage* S, int nb, const unsigned char* const* U, unsigned char* const* T, const int* n,
-                const int* idx);
+                const int* idx, const std::function<void()>* before_copy_out = nullptr);
 
 // Debug mode (environment QZGPU_DEBUG=1): every launch is followed by a
 // stream synchronize and an error check, and failures are logged to stderr.

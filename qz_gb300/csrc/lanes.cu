@@ -19,6 +19,8 @@ namespace qz {
 
 namespace {
 
+constexpr long long kTouchMinBytes = 8ll << 20;  // smaller host batches copy out directly
+
 int lanes_for(long long cap_bytes) {
     const char* env = getenv("QZGPU_LANES");
     if (env && atoi(env) > 0) return std::min(atoi(env), 16);
@@ -114,6 +116,32 @@ int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned cha
         off += bytes;
         b0 = b1;
     }
+    // Output pages of host buffers that nothing has touched yet (fresh
+    // allocations) make device-to-host copies fault page by page, several
+    // times slower than into resident pages.  A host thread touches one byte
+    // per page of every output buffer, in block order, while the device
+    // works; a lane waits for its blocks before it copies them out.
+    std::atomic<int> touched{nb};
+    std::mutex tmu;
+    std::condition_variable tcv;
+    std::thread toucher;
+    if (host && off >= kTouchMinBytes) {
+        touched = 0;
+        toucher = std::thread([&] {
+            for (int b = 0; b < nb; ++b) {
+                // in place (output = input): the caller's pages are resident
+                // and still hold the input
+                volatile unsigned char* p = hout[b];
+                if (hout[b] != hin[b])
+                    for (long long o = 0; o < n[b]; o += 4096) p[o] = 0;
+                {
+                    std::lock_guard<std::mutex> lk(tmu);
+                    touched.store(b + 1);
+                }
+                tcv.notify_all();
+            }
+        });
+    }
     const int K = (int)E->lanes.size();
     std::atomic<int> cursor{0};
     std::atomic<int> first_err{0};
@@ -128,8 +156,13 @@ int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned cha
         const int cnt = sb.b1 - sb.b0;
         int rc;
         if (host) {
-            rc = forward ? encode_host(S, cnt, hin + sb.b0, hout + sb.b0, n + sb.b0, idx + sb.b0, nullptr, nullptr)
-                         : decode_host(S, cnt, hin + sb.b0, hout + sb.b0, n + sb.b0, idx + sb.b0);
+            const std::function<void()> wait_out = [&] {
+                std::unique_lock<std::mutex> lk(tmu);
+                tcv.wait(lk, [&] { return touched.load() >= sb.b1; });
+            };
+            rc = forward ? encode_host(S, cnt, hin + sb.b0, hout + sb.b0, n + sb.b0, idx + sb.b0, nullptr, nullptr,
+                                       &wait_out)
+                         : decode_host(S, cnt, hin + sb.b0, hout + sb.b0, n + sb.b0, idx + sb.b0, &wait_out);
         } else {
             rc = forward ? forward_run(S, cnt, n + sb.b0, d_in + sb.off, d_out + sb.off, idx + sb.b0, nullptr,
                                        nullptr, S->stream)
@@ -166,6 +199,7 @@ int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned cha
         E->dcv.wait(lk, [&] { return E->job_done == K; });
         E->job = nullptr;
     }
+    if (toucher.joinable()) toucher.join();
     // merge lane counters (round counts only for a forward call)
     E->stats = qzgpu_stats{};
     if (forward) E->rounds_active.clear();

@@ -374,7 +374,7 @@ int check_blocks(int nblocks, const int* n, long long* total) {
 
 // Host-buffer forward batch on storage S (caller holds S->mu).
 int encode_host(Storage* S, int nb, const unsigned char* const* T, unsigned char* const* U, const int* n,
-                int* idx, const int* aux_rate, int* aux_out) {
+                int* idx, const int* aux_rate, int* aux_out, const std::function<void()>* before_copy_out) {
     cudaError_t e = cudaSetDevice(S->device);
     if (e != cudaSuccess) return map_cuda_error(e);
     long long off = 0;
@@ -387,6 +387,7 @@ int encode_host(Storage* S, int nb, const unsigned char* const* T, unsigned char
     }
     int rc = forward_run(S, nb, n, S->T, S->U, idx, aux_rate, aux_out, S->stream);
     if (rc) return rc;
+    if (before_copy_out) (*before_copy_out)();
     off = 0;
     for (int b = 0; b < nb; ++b) {
         if (n[b] > 0) {
@@ -400,7 +401,7 @@ int encode_host(Storage* S, int nb, const unsigned char* const* T, unsigned char
 }
 
 int decode_host(Storage* S, int nb, const unsigned char* const* U, unsigned char* const* T, const int* n,
-                const int* idx) {
+                const int* idx, const std::function<void()>* before_copy_out) {
     cudaError_t e = cudaSetDevice(S->device);
     if (e != cudaSuccess) return map_cuda_error(e);
     long long off = 0;
@@ -413,6 +414,7 @@ int decode_host(Storage* S, int nb, const unsigned char* const* U, unsigned char
     }
     int rc = inverse_run(S, nb, n, idx, S->U, S->T, S->stream);
     if (rc) return rc;
+    if (before_copy_out) (*before_copy_out)();
     off = 0;
     for (int b = 0; b < nb; ++b) {
         if (n[b] > 0) {

@@ -188,3 +188,60 @@ def test_profile_only_times_one_kernel(gpu):
         st.encode_batch(blocks)
         assert len(st.profile_read()) > 3
         st.profile(False)
+
+
+def _big_blocks():
+    g = synth.uniform_genome(400_000, seed=91)
+    return [synth.sample_reads(g, 20_000, seed=92 + i) for i in range(3)]  # 3 x 3 MB
+
+
+def test_batch_fresh_outputs_above_touch_threshold(gpu, oracle):
+    # more than 8 MiB of host output: the engine touches the output pages on a
+    # host thread while the device works
+    blocks = _big_blocks()
+    with bwt.Storage(sum(len(b) for b in blocks), len(blocks)) as st:
+        us, idx = st.encode_batch(blocks)
+        ous, oidx = oracle.bwt_encode_batch(blocks)
+        assert idx == list(oidx)
+        assert all((u == ou).all() for u, ou in zip(us, ous))
+        back = st.decode_batch(us, idx)
+        assert all((x == y).all() for x, y in zip(back, blocks))
+
+
+def test_batch_in_place_above_touch_threshold(gpu, oracle):
+    import ctypes
+    blocks = _big_blocks()
+    work = [b.copy() for b in blocks]
+    nb = len(work)
+    sizes = np.array([len(b) for b in work], dtype=np.int32)
+    idx = np.zeros(nb, dtype=np.int32)
+    u8p = ctypes.POINTER(ctypes.c_uint8)
+    ptrs = (u8p * nb)(*[b.ctypes.data_as(u8p) for b in work])
+    with bwt.Storage(int(sizes.sum()), nb) as st:
+        lib = native.load()
+        i32p = ctypes.POINTER(ctypes.c_int32)
+        rc = lib.qzgpu_bwt_encode_batch(st._h, nb, ptrs, ptrs, sizes.ctypes.data_as(i32p), idx.ctypes.data_as(i32p), 0)
+        assert rc == 0
+        ous, oidx = oracle.bwt_encode_batch(blocks)
+        assert list(idx) == list(oidx)
+        assert all((w == ou).all() for w, ou in zip(work, ous))
+        rc = lib.qzgpu_bwt_decode_batch(st._h, nb, ptrs, ptrs, sizes.ctypes.data_as(i32p), idx.ctypes.data_as(i32p), 0)
+        assert rc == 0
+        assert all((w == b).all() for w, b in zip(work, blocks))
+
+
+def test_batch_out_buffers_reused(gpu):
+    blocks = [synth.quality_stream(2000, seed=95), synth.header_stream(3000, seed=96), np.zeros(0, np.uint8)]
+    with bwt.Storage(sum(len(b) for b in blocks), len(blocks)) as st:
+        us0, idx0 = st.encode_batch(blocks)
+        outs = [np.empty(len(b), np.uint8) for b in blocks]
+        back = [np.empty(len(b), np.uint8) for b in blocks]
+        for _ in range(2):
+            us, idx = st.encode_batch(blocks, out=outs)
+            assert idx[:2] == idx0[:2]
+            assert all((u == v).all() for u, v in zip(us, us0))
+            assert all(u.base is o or u is o or np.shares_memory(u, o) for u, o in zip(us[:2], outs[:2]))
+            st.decode_batch(us, idx, out=back)
+            assert all((x == y).all() for x, y in zip(back, blocks))
+        with pytest.raises(native.QzGpuError):
+            st.encode_batch(blocks, out=outs[:2])
