@@ -95,6 +95,25 @@ __device__ __forceinline__ int block_incl_max(int v, int* sh, int* total) {
     return res;
 }
 
+// Rank-array accesses with an L2 evict-last policy: the random rank gathers and
+// scatters of a round reuse the same array, while the slot arrays stream
+// through with evict-first hints.
+__device__ __forceinline__ unsigned long long l2_keep_policy() {
+    unsigned long long pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+__device__ __forceinline__ int ld_keep(const int* p, unsigned long long pol) {
+    int v;
+    asm volatile("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
+__device__ __forceinline__ void st_keep(int* p, int v, unsigned long long pol) {
+    asm volatile("st.global.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
+}
+
 // Index of the block that owns global position x: off[b] <= x < off[b+1].
 __device__ __forceinline__ int block_of(const int* __restrict__ off, int nblocks, int x) {
     int lo = 0, hi = nblocks - 1;

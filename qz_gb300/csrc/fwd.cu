@@ -160,10 +160,10 @@ __device__ __forceinline__ BlockSpan block_span(const GatherArgs& g, int x) {
 __device__ __forceinline__ uint32_t rank_key(const GatherArgs& g, const BlockSpan& s, int x) {
     int i = x - s.bs;
     if (g.round == 0) {
-        if ((long long)i + s.h < s.n) return (uint32_t)__ldg(g.R + x + (int)s.h);
+        if ((long long)i + s.h < s.n) return (uint32_t)ld_keep(g.R + x + (int)s.h, l2_keep_policy());
         return s.h >= s.n ? (uint32_t)(s.n - i) : 0u;
     }
-    if ((long long)i + s.h < s.n) return (uint32_t)__ldg(g.R + x + (int)s.h) + (uint32_t)s.h + 1u;
+    if ((long long)i + s.h < s.n) return (uint32_t)ld_keep(g.R + x + (int)s.h, l2_keep_policy()) + (uint32_t)s.h + 1u;
     return (uint32_t)(s.n - i);
 }
 
@@ -829,7 +829,8 @@ __global__ void __launch_bounds__(kThreads, 5) k_split_apply(SplitArgs a) {
                 int w = t.w[i];
                 int g = t.g[i];
                 int rank = g + (ks - kg);
-                if (a.write_rank == kRankAll || (a.write_rank == kRankChanged && rank != g)) a.R[w] = rank;
+                if (a.write_rank == kRankAll || (a.write_rank == kRankChanged && rank != g))
+                    st_keep(a.R + w, rank, l2_keep_policy());
                 if (single) {
                     a.SA[g + (kk - kg)] = w;
                 } else {
@@ -862,7 +863,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_split_apply(SplitArgs a) {
 __global__ void __launch_bounds__(kThreads) k_rank_fixup(int N, const int* __restrict__ SA, int* __restrict__ R) {
     for (int j = blockIdx.x * kThreads + threadIdx.x; j < N; j += gridDim.x * kThreads) {
         int s = __ldcs(SA + j);
-        if (s >= 0) R[s] = j;
+        if (s >= 0) st_keep(R + s, j, l2_keep_policy());
     }
 }
 
