@@ -59,6 +59,7 @@ struct FwdBuffers {
     uint8_t* straddle;  // per 32-slot window: a small group may cross its right boundary
     uint32_t* h4;      // large groups: digit counts of all four passes
     unsigned long long* status64;  // look-back status per (tile, digit)
+    uint32_t* gmask;   // large: per group, the passes whose digit is not constant
     uint32_t* ltc;     // large: tiles per group -> tile base
     uint32_t* llen;    // large: length per group -> workspace base
     uint32_t* ltbase;
@@ -85,7 +86,7 @@ struct Tune {
     int big_ctas_per_sm = 4;   // persistent CTAs of a look-back radix pass
     int tile_ctas_per_sm = 3;  // CTAs of the one-CTA group sort
     int medium_max = kMedMax;  // longest group sorted by one warp (64..512)
-    int ruler_log2 = 5;        // inverse: a ruler every 2^ruler_log2 rows (3..7)
+    int ruler_log2 = 5;        // inverse: a ruler every 2^ruler_log2 rows (3..12)
 };
 
 struct Storage {

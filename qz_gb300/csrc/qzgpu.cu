@@ -192,6 +192,7 @@ size_t layout(Storage* S, char* base, const Caps& c) {
     f.list_large = cv.take<int2>(c.large);
     f.h4 = cv.take<uint32_t>(1024 * c.large);
     f.status64 = cv.take<unsigned long long>(256 * c.big_tiles);
+    f.gmask = cv.take<uint32_t>(c.large + 1);
     f.ltc = cv.take<uint32_t>(c.large + 1);
     f.llen = cv.take<uint32_t>(c.large + 1);
     f.ltbase = cv.take<uint32_t>(c.large + 1);
@@ -625,7 +626,7 @@ int qzgpu_storage_set_param(qzgpu_storage* storage, const char* name, long long 
         if (value != 64 && value != 128 && value != 256 && value != 512) return QZGPU_BAD_PARAMETER;
         each([&](Tune& t) { t.medium_max = (int)value; });
     } else if (k == "ruler_stride_log2") {
-        if (value < 3 || value > 7) return QZGPU_BAD_PARAMETER;
+        if (value < 3 || value > 12) return QZGPU_BAD_PARAMETER;
         each([&](Tune& t) { t.ruler_log2 = (int)value; });
     } else {
         return QZGPU_BAD_PARAMETER;

@@ -147,12 +147,14 @@ __global__ void __launch_bounds__(kThreads) k_tile_sort(const int2* __restrict__
 // ------------------------------------------------------------------ multi-tile groups
 
 __global__ void __launch_bounds__(kThreads) k_big_prep(const int2* __restrict__ list, const int* __restrict__ d_count,
-                                                       uint32_t* __restrict__ tcount, uint32_t* __restrict__ lens) {
+                                                       uint32_t* __restrict__ tcount, uint32_t* __restrict__ lens,
+                                                       uint32_t* __restrict__ gmask) {
     int cnt = *d_count;
     for (int i = blockIdx.x * kThreads + threadIdx.x; i < cnt; i += gridDim.x * kThreads) {
         int len = list[i].y;
         tcount[i] = (uint32_t)((len + kOT - 1) / kOT);
         lens[i] = (uint32_t)len;
+        gmask[i] = 0;
     }
 }
 
@@ -197,23 +199,129 @@ __global__ void __launch_bounds__(kThreads) k_big_hist(BigArgs a, const uint32_t
     }
 }
 
-// Per group and pass: exclusive prefix over the 256 digits (in place).
-__global__ void __launch_bounds__(kThreads) k_big_bases(const int* __restrict__ d_nseg, uint32_t* __restrict__ h4) {
+// Per group and pass: exclusive prefix over the 256 digits (in place), and
+// the pass is marked needed unless one digit holds the whole group.
+__global__ void __launch_bounds__(kThreads) k_big_bases(BigArgs a, uint32_t* __restrict__ h4) {
     __shared__ uint32_t sh[kWarps + 1];
-    int n = *d_nseg * 4;
+    int n = *a.nseg * 4;
     for (int r = blockIdx.x; r < n; r += gridDim.x) {
         uint32_t v = h4[(size_t)r * 256 + threadIdx.x];
+        const uint32_t len = (uint32_t)a.list[r >> 2].y;
+        const bool whole = __syncthreads_or(v == len);
         uint32_t tot;
         h4[(size_t)r * 256 + threadIdx.x] = block_excl_sum(v, sh, &tot);
+        if (threadIdx.x == 0 && !whole) atomicOr(&a.gmask[r >> 2], 1u << (r & 3));
+    }
+}
+
+// Passes a group runs: those whose digit is not constant, plus one trivial
+// pass when that leaves a single one, so that no pass reads and writes the
+// compact arrays at once.  The added pass leaves the order that matters: pass
+// 0 (unstable) before a stable pass on the only varying digit, or the stable
+// pass 1 after an only pass 0.
+__device__ __forceinline__ uint32_t big_passes(uint32_t m) {
+    return __popc(m) == 1 ? (m | (m == 1u ? 2u : 1u)) : m;
+}
+
+// Buffers of group s for pass p (a needed pass of its mask m).
+struct BigRoute {
+    const uint32_t* sk;
+    const int* sv;
+    uint32_t* dk;
+    int* dv;
+};
+
+__device__ __forceinline__ BigRoute big_route(const BigBuffers& bb, const int2 d, uint32_t wb, uint32_t m, int p) {
+    const int k = __popc(m & ((1u << p) - 1u));  // needed passes before this one
+    const bool last = (m >> (p + 1)) == 0;
+    // selects, not indexing, so the parameter arrays stay in registers
+    const bool sodd = ((k - 1) & 1) != 0, dodd = (k & 1) != 0;
+    BigRoute r;
+    r.sk = k == 0 ? bb.key + d.x : (sodd ? bb.wsk[1] : bb.wsk[0]) + wb;
+    r.sv = k == 0 ? bb.val + d.x : (sodd ? bb.wsv[1] : bb.wsv[0]) + wb;
+    r.dk = last ? bb.key + d.x : (dodd ? bb.wsk[1] : bb.wsk[0]) + wb;
+    r.dv = last ? bb.val + d.x : (dodd ? bb.wsv[1] : bb.wsv[0]) + wb;
+    return r;
+}
+
+// Pass 0 (bits 0..7).  Equal keys may leave a group sort in any order (the
+// split gives them one rank), so this pass needs no stability: a tile ranks its
+// slots with shared-memory atomics and reserves each digit's output range with
+// one atomic on the group's digit cursor (its pass-0 base row), so it neither
+// matches nor looks back.
+__global__ void __launch_bounds__(kThreads, 3) k_big_pass0(BigArgs a, uint32_t* __restrict__ h4, BigBuffers bb) {
+    __shared__ uint32_t skey[kOT];
+    __shared__ int sval[kOT];
+    __shared__ uint32_t cnt[256];
+    __shared__ uint32_t gb[256];
+    __shared__ uint32_t sh[kWarps + 1];
+    __shared__ int s_seg;
+    const unsigned w = warp_id(), ln = lane_id();
+    const int TT = *a.ntiles, nseg = *a.nseg;
+    for (int tau = blockIdx.x; tau < TT; tau += gridDim.x) {
+        if (threadIdx.x == 0) s_seg = big_seg_of_tile(a.tbase, nseg, (uint32_t)tau);
+        cnt[threadIdx.x] = 0;
+        __syncthreads();
+        const int s = s_seg;
+        const uint32_t m = big_passes(a.gmask[s]);
+        if (!(m & 1u)) {
+            __syncthreads();
+            continue;  // uniform across the CTA
+        }
+        const int2 d = a.list[s];
+        const int j = tau - (int)a.tbase[s];
+        const uint32_t wb = a.wbase[s];
+        const BigRoute rt = big_route(bb, d, wb, m, 0);
+        const uint32_t* sk = rt.sk;
+        const int* sv = rt.sv;
+        uint32_t* dk = rt.dk;
+        int* dv = rt.dv;
+        const int src = j * kOT;
+        const int n = min(kOT, d.y - j * kOT);
+        uint32_t kr[kOItems], rk[kOItems];
+#pragma unroll
+        for (int it = 0; it < kOItems; ++it) {
+            int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
+            kr[it] = i < n ? __ldcs(sk + src + i) : 0u;
+        }
+#pragma unroll
+        for (int it = 0; it < kOItems; ++it) {
+            int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
+            rk[it] = i < n ? atomicAdd(&cnt[kr[it] & 255u], 1u) : 0u;
+        }
+        __syncthreads();
+        {
+            const uint32_t c = cnt[threadIdx.x];
+            const uint32_t base = c ? atomicAdd(&h4[(size_t)s * 1024 + threadIdx.x], c) : 0u;
+            uint32_t tot;
+            const uint32_t off = block_excl_sum(c, sh, &tot);
+            cnt[threadIdx.x] = off;
+            gb[threadIdx.x] = base - off;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int it = 0; it < kOItems; ++it) {
+            int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
+            if (i < n) {
+                uint32_t lp = cnt[kr[it] & 255u] + rk[it];
+                skey[lp] = kr[it];
+                sval[lp] = __ldcs(sv + src + i);
+            }
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += kThreads) {
+            uint32_t kv = skey[i];
+            uint32_t dst = gb[kv & 255u] + (uint32_t)i;
+            dk[dst] = kv;
+            dv[dst] = sval[i];
+        }
+        __syncthreads();
     }
 }
 
 // One stable 8-bit pass with decoupled look-back.
-__global__ void __launch_bounds__(kThreads) k_big_pass(BigArgs a, const uint32_t* __restrict__ h4, int pass,
-                                                       unsigned epoch, const uint32_t* __restrict__ srck,
-                                                       const int* __restrict__ srcv, int src_compact,
-                                                       uint32_t* __restrict__ dstk, int* __restrict__ dstv,
-                                                       int dst_compact, unsigned long long* status,
+__global__ void __launch_bounds__(kThreads, 4) k_big_pass(BigArgs a, const uint32_t* __restrict__ h4, int pass,
+                                                       unsigned epoch, BigBuffers bb, unsigned long long* status,
                                                        unsigned* ticket, DevStatus* st) {
     __shared__ uint32_t skey[kOT];
     __shared__ int sval[kOT];
@@ -238,17 +346,34 @@ __global__ void __launch_bounds__(kThreads) k_big_pass(BigArgs a, const uint32_t
         int tau = s_tau;
         if (tau >= TT) return;
         int s = s_seg;
+        const uint32_t m = big_passes(a.gmask[s]);
+        if (!(m >> pass & 1u)) {
+            // nothing to sort on this digit: the group's slots stay put and no
+            // tile of it looks back at this one
+            __syncthreads();
+            continue;
+        }
         int2 d = a.list[s];
         int j = tau - (int)a.tbase[s];
-        int srcbase = (src_compact ? d.x : (int)a.wbase[s]) + j * kOT;
-        int dstseg = dst_compact ? d.x : (int)a.wbase[s];
+        const BigRoute rt = big_route(bb, d, a.wbase[s], m, pass);
+        const uint32_t* srck = rt.sk;
+        const int* srcv = rt.sv;
+        uint32_t* dstk = rt.dk;
+        int* dstv = rt.dv;
+        int srcbase = j * kOT;
         int cnt = min(kOT, d.y - j * kOT);
-        uint32_t rk[kOItems];
+        uint32_t rk[kOItems], kr[kOItems];
+        // all of the tile's keys in flight at once, then the ranking
+#pragma unroll
+        for (int it = 0; it < kOItems; ++it) {
+            int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
+            kr[it] = i < cnt ? __ldg(srck + srcbase + i) : 0u;
+        }
 #pragma unroll
         for (int it = 0; it < kOItems; ++it) {
             int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
             bool valid = i < cnt;
-            uint32_t kv = valid ? srck[srcbase + i] : 0u;
+            uint32_t kv = kr[it];
             unsigned dg = valid ? (kv >> shift) & 255u : 256u;
             unsigned peers = __match_any_sync(0xffffffffu, dg);
             unsigned before = __popc(peers & lt_mask);
@@ -298,18 +423,18 @@ __global__ void __launch_bounds__(kThreads) k_big_pass(BigArgs a, const uint32_t
             }
             uint32_t tot;
             dig_off[dg] = block_excl_sum(run, sh, &tot);
-            gbase[dg] = (uint32_t)dstseg + h4[((size_t)s * 4 + pass) * 256 + dg] + excl;
+            gbase[dg] = h4[((size_t)s * 4 + pass) * 256 + dg] + excl;
         }
         __syncthreads();
 #pragma unroll
         for (int it = 0; it < kOItems; ++it) {
             int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
             if (i < cnt) {
-                uint32_t kv = srck[srcbase + i];
+                uint32_t kv = kr[it];
                 unsigned dg = (kv >> shift) & 255u;
                 uint32_t lp = dig_off[dg] + wcnt[w][dg] + rk[it];
                 skey[lp] = kv;
-                sval[lp] = srcv[srcbase + i];
+                sval[lp] = __ldg(srcv + srcbase + i);
             }
         }
         __syncthreads();
@@ -352,32 +477,33 @@ void sort_big_groups(Storage* S, const int2* list, const int* d_count, int host_
     FwdBuffers& f = S->f;
     int* cnt = S->counters;
     const int sms = S->sms;
-    QZ_LAUNCH(S, st, "k_big_prep", 16ll * host_count,
-              k_big_prep<<<grid_cap(host_count, kThreads, sms * 4), kThreads, 0, st>>>(list, d_count, f.ltc, f.llen));
+    QZ_LAUNCH(S, st, "k_big_prep", 20ll * host_count,
+              k_big_prep<<<grid_cap(host_count, kThreads, sms * 4), kThreads, 0, st>>>(list, d_count, f.ltc, f.llen,
+                                                                                      f.gmask));
     scan_exclusive(S, f.ltc, f.ltbase, 0, d_count, (uint32_t*)(cnt + CNT_LTILES), st);
     scan_exclusive(S, f.llen, f.lwbase, 0, d_count, nullptr, st);
-    BigArgs a{list, d_count, f.ltbase, f.lwbase, cnt + CNT_LTILES};
+    BigArgs a{list, d_count, f.ltbase, f.lwbase, cnt + CNT_LTILES, f.gmask};
+    BigBuffers bb{key, val, {f.wsk[0], f.wsk[1]}, {f.wsv[0], f.wsv[1]}};
     uint32_t* h4 = f.h4;
     cudaMemsetAsync(h4, 0, sizeof(uint32_t) * 1024 * (size_t)host_count, st);
     int grid = sms * 4;
     QZ_LAUNCH(S, st, "k_big_hist", 4 * elems, k_big_hist<<<grid, kThreads, 0, st>>>(a, key, h4));
     QZ_LAUNCH(S, st, "k_big_bases", 4096ll * host_count,
-              k_big_bases<<<grid_cap(4ll * host_count, 1, sms * 8), kThreads, 0, st>>>(d_count, h4));
-    const uint32_t* sk[4] = {key, f.wsk[0], f.wsk[1], f.wsk[0]};
-    const int* sv[4] = {val, f.wsv[0], f.wsv[1], f.wsv[0]};
-    uint32_t* dk[4] = {f.wsk[0], f.wsk[1], f.wsk[0], key};
-    int* dv[4] = {f.wsv[0], f.wsv[1], f.wsv[0], val};
-    // persistent grid of resident CTAs (64 registers and 43 KB of shared
-    // memory per CTA fit four per SM); tiles are taken by ticket
+              k_big_bases<<<grid_cap(4ll * host_count, 1, sms * 8), kThreads, 0, st>>>(a, h4));
+    // pass 0: unstable, no look-back (bytes are an upper bound: passes whose
+    // digit is constant in a group are skipped for that group)
+    QZ_LAUNCH(S, st, "k_big_pass0", 16 * elems, k_big_pass0<<<grid, kThreads, 0, st>>>(a, h4, bb));
+    // passes 1..3: stable, decoupled look-back; a persistent grid of resident
+    // CTAs (64 registers and 43 KB of shared memory per CTA fit four per SM),
+    // tiles taken by ticket
     int pgrid = sms * S->tune.big_ctas_per_sm;
-    for (int pass = 0; pass < 4; ++pass) {
+    for (int pass = 1; pass < 4; ++pass) {
         unsigned epoch = ++S->radix_epoch & 0x3fffffffu;
         if (epoch == 0) epoch = ++S->radix_epoch & 0x3fffffffu;
         unsigned* ticket = reinterpret_cast<unsigned*>(cnt + CNT_TICKET);
         cudaMemsetAsync(ticket, 0, sizeof(unsigned), st);
         QZ_LAUNCH(S, st, "k_big_pass", 16 * elems,
-                  k_big_pass<<<pgrid, kThreads, 0, st>>>(a, h4, pass, epoch, sk[pass], sv[pass], pass == 0, dk[pass],
-                                                         dv[pass], pass == 3, f.status64, ticket, S->status));
+                  k_big_pass<<<pgrid, kThreads, 0, st>>>(a, h4, pass, epoch, bb, f.status64, ticket, S->status));
     }
 }
 

@@ -10,6 +10,17 @@ struct BigArgs {
     const uint32_t* tbase;   // first tile of each group
     const uint32_t* wbase;   // first workspace slot of each group
     const int* ntiles;       // total tiles (device)
+    uint32_t* gmask;         // per group: passes whose digit is not constant (bit p)
+};
+
+// Where a group's slots are before / after one of its needed passes: the first
+// needed pass reads the compact (key, val) arrays, the last writes them back,
+// the others ping-pong through the two workspaces.
+struct BigBuffers {
+    uint32_t* key;
+    int* val;
+    uint32_t* wsk[2];
+    int* wsv[2];
 };
 
 // Groups of kMedMax+1 .. kOT slots (one CTA each, all passes in shared memory).
