@@ -50,9 +50,15 @@ __global__ void __launch_bounds__(kThreads) k_inv_up(InvArgs a, uint32_t* __rest
     int j = (s0 - bs) / kInitTile;
     int m = (n + kInitTile - 1) / kInitTile;
     int end = min(bs + n, s0 + kInitTile);
-    for (int base = s0; base < end; base += kThreads) {
-        int x = base + threadIdx.x;
-        unsigned c = x < end ? (unsigned)a.U[x] : 256u;
+    unsigned cu[kInitTile / kThreads];
+#pragma unroll
+    for (int it = 0; it < kInitTile / kThreads; ++it) {
+        int x = s0 + it * kThreads + threadIdx.x;
+        cu[it] = x < end ? (unsigned)__ldg(a.U + x) : 256u;
+    }
+#pragma unroll
+    for (int it = 0; it < kInitTile / kThreads; ++it) {
+        unsigned c = cu[it];
         unsigned peers = __match_any_sync(0xffffffffu, c);
         if (c < 256u && lane_id() == (unsigned)(__ffs(peers) - 1)) atomicAdd(&h[c], __popc(peers));
     }
@@ -78,11 +84,18 @@ __global__ void __launch_bounds__(kThreads) k_inv_down(InvArgs a, const uint32_t
     __syncthreads();
     uint8_t cc[kIRItems];
     uint32_t rk[kIRItems];
+    unsigned cu[kIRItems];
+    // all of the tile's symbols in flight at once, then the ranking
+#pragma unroll
+    for (int it = 0; it < kIRItems; ++it) {
+        int i = (int)w * kIRWarpSpan + it * 32 + (int)ln;
+        cu[it] = i < cnt ? (unsigned)__ldg(a.U + s0 + i) : 256u;
+    }
 #pragma unroll
     for (int it = 0; it < kIRItems; ++it) {
         int i = (int)w * kIRWarpSpan + it * 32 + (int)ln;
         bool valid = i < cnt;
-        unsigned c = valid ? (unsigned)a.U[s0 + i] : 256u;
+        unsigned c = cu[it];
         unsigned peers = __match_any_sync(0xffffffffu, c);
         unsigned before = __popc(peers & lt_mask);
         uint32_t prev = valid ? wcnt[w][c] : 0u;

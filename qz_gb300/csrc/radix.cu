@@ -184,10 +184,18 @@ __global__ void __launch_bounds__(kThreads) k_big_hist(BigArgs a, const uint32_t
         int j = tau - (int)a.tbase[s];
         int base = d.x + j * kOT;
         int cnt = min(kOT, d.y - j * kOT);
-        for (int i = threadIdx.x; i < cnt; i += kThreads) {
-            uint32_t kv = key[base + i];
+        uint32_t kr[kOItems];
 #pragma unroll
-            for (int p = 0; p < 4; ++p) atomicAdd(&h[p][(kv >> (8 * p)) & 255u], 1u);
+        for (int it = 0; it < kOItems; ++it) {
+            int i = it * kThreads + threadIdx.x;
+            kr[it] = i < cnt ? __ldg(key + base + i) : 0u;
+        }
+#pragma unroll
+        for (int it = 0; it < kOItems; ++it) {
+            if (it * kThreads + (int)threadIdx.x < cnt) {
+#pragma unroll
+                for (int p = 0; p < 4; ++p) atomicAdd(&h[p][(kr[it] >> (8 * p)) & 255u], 1u);
+            }
         }
         __syncthreads();
 #pragma unroll
