@@ -38,24 +38,51 @@ namespace qz {
 // ------------------------------------------------------------------ per-block alphabet
 
 __global__ void __launch_bounds__(kThreads) k_block_hist(const uint8_t* __restrict__ T,
-                                                         const int2* __restrict__ tiles,
+                                                         const int2* __restrict__ tiles, int ntiles,
                                                          const int* __restrict__ off,
                                                          uint32_t* __restrict__ bhist) {
-    __shared__ uint32_t h[256];
-    h[threadIdx.x] = 0;
+    // each CTA counts a contiguous run of tiles into per-warp shared
+    // histograms, all of a tile's bytes loaded before counting, and flushes
+    // when the block changes
+    __shared__ uint32_t h[kWarps][256];
+    int lo, hi;
+    chunk_range(ntiles, gridDim.x, blockIdx.x, 1, &lo, &hi);
+    if (lo >= hi) return;
+#pragma unroll
+    for (int q = 0; q < kWarps; ++q) h[q][threadIdx.x] = 0;
     __syncthreads();
-    int2 tl = tiles[blockIdx.x];
-    int b = tl.x, s0 = tl.y;
-    int end = min(off[b + 1], s0 + kInitTile);
-    for (int base = s0; base < end; base += kThreads) {
-        int x = base + threadIdx.x;
-        unsigned c = x < end ? (unsigned)T[x] : 256u;
-        unsigned peers = __match_any_sync(0xffffffffu, c);
-        if (c < 256u && lane_id() == (unsigned)(__ffs(peers) - 1)) atomicAdd(&h[c], __popc(peers));
+    constexpr int kPer = kInitTile / kThreads;
+    int cur = tiles[lo].x;
+    for (int t = lo; t < hi; ++t) {
+        const int2 tl = tiles[t];
+        if (tl.x != cur) {  // uniform across the CTA
+            __syncthreads();
+            uint32_t v = 0;
+#pragma unroll
+            for (int q = 0; q < kWarps; ++q) {
+                v += h[q][threadIdx.x];
+                h[q][threadIdx.x] = 0;
+            }
+            if (v) atomicAdd(&bhist[(size_t)cur * 256 + threadIdx.x], v);
+            cur = tl.x;
+            __syncthreads();
+        }
+        const int end = min(off[tl.x + 1], tl.y + kInitTile);
+        unsigned c[kPer];
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            const int x = tl.y + k * kThreads + threadIdx.x;
+            c[k] = x < end ? (unsigned)__ldcs(T + x) : 256u;
+        }
+#pragma unroll
+        for (int k = 0; k < kPer; ++k)
+            if (c[k] < 256u) atomicAdd(&h[warp_id()][c[k]], 1u);
     }
     __syncthreads();
-    uint32_t v = h[threadIdx.x];
-    if (v) atomicAdd(&bhist[(size_t)b * 256 + threadIdx.x], v);
+    uint32_t v = 0;
+#pragma unroll
+    for (int q = 0; q < kWarps; ++q) v += h[q][threadIdx.x];
+    if (v) atomicAdd(&bhist[(size_t)cur * 256 + threadIdx.x], v);
 }
 
 __global__ void __launch_bounds__(kThreads) k_block_alpha(const uint32_t* __restrict__ bhist,
@@ -1042,7 +1069,8 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
     // ---- alphabet, initial keys
     int ntiles = (int)tiles.size();
     QZ_LAUNCH(S, st, "k_block_hist", N,
-              k_block_hist<<<ntiles, kThreads, 0, st>>>(d_T, S->tiles, S->blk_off, S->blk_hist));
+              k_block_hist<<<grid_for(ntiles, 4, S->sms * 8), kThreads, 0, st>>>(d_T, S->tiles, ntiles, S->blk_off,
+                                                                                S->blk_hist));
     QZ_LAUNCH(S, st, "k_block_alpha", 1280ll * nb,
               k_block_alpha<<<nb, kThreads, 0, st>>>(S->blk_hist, S->blk_code, S->blk_K, S->blk_sigma));
     // reads T once, writes key, R (the same text key, in text order), W and G
