@@ -236,6 +236,8 @@ __global__ void __launch_bounds__(kThreads) k_inv_walk2(InvArgs a, RulerArgs r, 
         }
     };
     for (int t = 0; t < L; ++t) {
+        // the next row is loaded first; the symbol search below overlaps it
+        const int nxt = __ldg(LF + cur);
         int s = n - d;
         if (s < 0) {
             report(a.st, QZGPU_DATA_CORRUPT, 13, b);
@@ -259,7 +261,7 @@ __global__ void __launch_bounds__(kThreads) k_inv_walk2(InvArgs a, RulerArgs r, 
             word |= (uint32_t)lo << (8 * q);
             have |= 1u << q;
         }
-        cur = LF[cur];
+        cur = nxt;
         ++d;
     }
     flush();
