@@ -152,8 +152,9 @@ __global__ void __launch_bounds__(kThreads) k_inv_walk1(InvArgs a, RulerArgs r) 
     int cur = lq << a.stride_log2;
     int steps = 0;
     bool ok = true;
+    const unsigned long long pol = l2_keep_policy();
     do {
-        cur = LF[cur];
+        cur = ld_keep(LF + cur, pol);
         ++steps;
         if (cur < 0 || cur > n || steps > n + 1) {
             ok = false;
@@ -193,15 +194,34 @@ __global__ void __launch_bounds__(kThreads) k_inv_walk2(InvArgs a, RulerArgs r, 
                                                         const int* __restrict__ dist,
                                                         const uint32_t* __restrict__ hist,
                                                         uint8_t* __restrict__ T) {
-    __shared__ int C[257];
+    __shared__ int C[257];       // first row of each present symbol, then n + 1
+    __shared__ uint8_t sym[256];  // the present symbols, ascending
+    __shared__ int s_cnt[kWarps + 1];
     int2 rt = r.rtiles[blockIdx.x];
     int b = rt.x;
     int bs = a.off[b], n = a.off[b + 1] - bs;
     int m = (n + kInitTile - 1) / kInitTile;
-    // symbol starts in the first column: 1 + count of smaller symbols
-    C[threadIdx.x] = (int)(hist[(size_t)256 * a.tbase[b] + (size_t)threadIdx.x * m] - (uint32_t)bs) + 1;
-    if (threadIdx.x == 0) C[256] = n + 1;
+    // symbol starts in the first column (1 + count of smaller symbols), kept
+    // for the symbols that occur only, so the search below takes log2(sigma)
+    // steps
+    {
+        const uint32_t* hb = hist + (size_t)256 * a.tbase[b];
+        const int c0 = (int)(hb[(size_t)threadIdx.x * m] - (uint32_t)bs) + 1;
+        const int c1 = threadIdx.x < 255 ? (int)(hb[(size_t)(threadIdx.x + 1) * m] - (uint32_t)bs) + 1 : n + 1;
+        const bool present = c1 > c0;
+        int tot;
+        const int at = block_excl_sum(present ? 1 : 0, s_cnt, &tot);
+        if (present) {
+            C[at] = c0;
+            sym[at] = (uint8_t)threadIdx.x;
+        }
+        if (threadIdx.x == 0) {
+            C[tot] = n + 1;
+            s_cnt[kWarps] = tot;
+        }
+    }
     __syncthreads();
+    const int sigma = s_cnt[kWarps];
     int M = (n >> a.stride_log2) + 1;
     int lq = rt.y + threadIdx.x;
     if (lq >= M) return;
@@ -223,6 +243,7 @@ __global__ void __launch_bounds__(kThreads) k_inv_walk2(InvArgs a, RulerArgs r, 
     // their absolute address, so the run leaves as word stores; a word not
     // completely filled by this walk is stored byte by byte.
     uint8_t* out = T + bs;
+    const unsigned long long pol = l2_keep_policy();
     uintptr_t word_at = 0;  // address of the word being filled (0: none)
     uint32_t word = 0;
     unsigned have = 0;      // bytes of that word filled so far (bit mask)
@@ -237,18 +258,19 @@ __global__ void __launch_bounds__(kThreads) k_inv_walk2(InvArgs a, RulerArgs r, 
     };
     for (int t = 0; t < L; ++t) {
         // the next row is loaded first; the symbol search below overlaps it
-        const int nxt = __ldg(LF + cur);
+        const int nxt = ld_keep(LF + cur, pol);
         int s = n - d;
         if (s < 0) {
             report(a.st, QZGPU_DATA_CORRUPT, 13, b);
             return;
         }
         if (s < n) {
-            int lo = 0, hi = 255;
+            int lo = 0, hi = sigma - 1;
             while (lo < hi) {
                 int mid = (lo + hi + 1) >> 1;
                 if (C[mid] <= cur) lo = mid; else hi = mid - 1;
             }
+            lo = sym[lo];
             uintptr_t addr = reinterpret_cast<uintptr_t>(out + s);
             uintptr_t wa = addr & ~(uintptr_t)3;
             if (wa != word_at) {
