@@ -146,7 +146,7 @@ int qzgpu_storage_round_counts(const qzgpu_storage *storage, long long *active, 
  *   "big_ctas_per_sm"                 persistent CTAs per SM of a radix pass (1..4)
  *   "tile_ctas_per_sm"                CTAs per SM of the one-CTA group sort (1..3)
  *   "medium_max"                      longest group sorted by one warp (64..512)
- *   "ruler_stride_log2"               inverse: a ruler every 2^v rows (3..7)
+ *   "ruler_stride_log2"               inverse: a ruler every 2^v rows (3..12)
  * get_param also answers "lanes".  Returns 0 / the value, or QZGPU_BAD_PARAMETER
  * for an unknown name or an out-of-range value.  No counterpart in libbsc. */
 int qzgpu_storage_set_param(qzgpu_storage *storage, const char *name, long long value);
