@@ -1,7 +1,8 @@
 // Batched calls on a multi-lane engine.
 //
-// A storage handed to callers (qzgpu_storage) is an engine of K lanes (two by
-// default: measured best on a 33-block chunk; QZGPU_LANES overrides).  Each
+// A storage handed to callers (qzgpu_storage) is an engine of K lanes (three
+// by default: measured best on a 33-block chunk and on 256 uneven blocks;
+// QZGPU_LANES overrides).  Each
 // lane is a full scratch set (Storage) with its own stream and a persistent
 // worker thread.  A batch is cut into sub-batches of at most lane_bytes block
 // bytes (blocks kept whole); lanes take sub-batches as they become free, so
@@ -24,7 +25,7 @@ constexpr long long kTouchMinBytes = 8ll << 20;  // smaller host batches copy ou
 int lanes_for(long long cap_bytes) {
     const char* env = getenv("QZGPU_LANES");
     if (env && atoi(env) > 0) return std::min(atoi(env), 16);
-    return cap_bytes > kLaneBytes ? 2 : 1;
+    return cap_bytes > kLaneBytes ? 3 : 1;
 }
 
 }  // namespace
