@@ -631,60 +631,67 @@ struct SplitArgs {
     int medium_max;    // longest group listed for the one-warp sort
 };
 
+// Lane l of a warp tile holds the 8 consecutive slots base + 8l .. base + 8l + 7,
+// so a slot's neighbours are in the lane's own registers except at its ends
+// (one shuffle each way); flags are bit masks over the lane's 8 slots.
 struct WarpTile {
     uint32_t k[kWI];
     int g[kWI];
     int w[kWI];
-    bool valid[kWI], gh[kWI], sh[kWI], nsh[kWI];
+    unsigned valid, gh, sh, nsh;
 };
+
+template <typename T>
+__device__ __forceinline__ void ld8(const T* __restrict__ p, int first, int A, T (&v)[kWI], T fill) {
+    static_assert(sizeof(T) == 4 && kWI == 8, "two 16-byte loads per lane");
+    if (first + kWI <= A) {
+        // first is a multiple of 8 and the arrays start 256-byte aligned
+        const uint4 a = __ldcs(reinterpret_cast<const uint4*>(p + first));
+        const uint4 b = __ldcs(reinterpret_cast<const uint4*>(p + first + 4));
+        const uint32_t u[kWI] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int i = 0; i < kWI; ++i) v[i] = (T)u[i];
+    } else {
+#pragma unroll
+        for (int i = 0; i < kWI; ++i) v[i] = first + i < A ? __ldcs(p + first + i) : fill;
+    }
+}
 
 template <bool WithSuffix>
 __device__ __forceinline__ void wt_load(const SplitArgs& a, int A, int base, WarpTile& t) {
-    const unsigned ln = lane_id();
+    const int ln = (int)lane_id();
+    const int first = base + kWI * ln;
+    ld8<uint32_t>(a.key, first, A, t.k, 0u);
+    ld8<int>(a.G, first, A, t.g, -1);
+    if (WithSuffix) ld8<int>(a.W, first, A, t.w, 0);
+    uint32_t pk = __shfl_up_sync(0xffffffffu, t.k[kWI - 1], 1);
+    int pg = __shfl_up_sync(0xffffffffu, t.g[kWI - 1], 1);
+    uint32_t nk = __shfl_down_sync(0xffffffffu, t.k[0], 1);
+    int ng = __shfl_down_sync(0xffffffffu, t.g[0], 1);
+    if (ln == 0) {
+        pk = base > 0 ? a.key[base - 1] : 0u;
+        pg = base > 0 ? a.G[base - 1] : -1;
+    }
+    if (ln == 31) {
+        nk = base + kWT < A ? a.key[base + kWT] : 0u;
+        ng = base + kWT < A ? a.G[base + kWT] : -1;
+    }
+    t.valid = t.gh = t.sh = t.nsh = 0;
 #pragma unroll
     for (int i = 0; i < kWI; ++i) {
-        int kk = base + 32 * i + (int)ln;
-        t.valid[i] = kk < A;
-        t.k[i] = t.valid[i] ? __ldcs(a.key + kk) : 0u;
-        t.g[i] = t.valid[i] ? __ldcs(a.G + kk) : -1;
-        if (WithSuffix) t.w[i] = t.valid[i] ? __ldcs(a.W + kk) : 0;
-    }
-    uint32_t pk = 0, nk = 0;
-    int pg = -1, ng = -1;
-    if (base > 0) {
-        pk = a.key[base - 1];
-        pg = a.G[base - 1];
-    }
-    if (base + kWT < A) {
-        nk = a.key[base + kWT];
-        ng = a.G[base + kWT];
-    }
-#pragma unroll
-    for (int i = 0; i < kWI; ++i) {
-        uint32_t prevk = __shfl_up_sync(0xffffffffu, t.k[i], 1);
-        int prevg = __shfl_up_sync(0xffffffffu, t.g[i], 1);
-        uint32_t lk = __shfl_sync(0xffffffffu, t.k[i > 0 ? i - 1 : 0], 31);
-        int lg = __shfl_sync(0xffffffffu, t.g[i > 0 ? i - 1 : 0], 31);
-        if (ln == 0) {
-            prevk = i > 0 ? lk : pk;
-            prevg = i > 0 ? lg : pg;
-        }
-        int kk = base + 32 * i + (int)ln;
-        t.gh[i] = t.valid[i] && (kk == 0 || prevg != t.g[i]);
-        t.sh[i] = t.valid[i] && (t.gh[i] || prevk != t.k[i]);
-    }
-#pragma unroll
-    for (int i = 0; i < kWI; ++i) {
-        uint32_t nxk = __shfl_down_sync(0xffffffffu, t.k[i], 1);
-        int nxg = __shfl_down_sync(0xffffffffu, t.g[i], 1);
-        uint32_t fk = __shfl_sync(0xffffffffu, t.k[i + 1 < kWI ? i + 1 : i], 0);
-        int fg = __shfl_sync(0xffffffffu, t.g[i + 1 < kWI ? i + 1 : i], 0);
-        if (ln == 31) {
-            nxk = i + 1 < kWI ? fk : nk;
-            nxg = i + 1 < kWI ? fg : ng;
-        }
-        int kk = base + 32 * i + (int)ln;
-        t.nsh[i] = kk + 1 >= A || nxg != t.g[i] || nxk != t.k[i];
+        const int kk = first + i;
+        const bool v = kk < A;
+        const uint32_t prk = i > 0 ? t.k[i - 1] : pk;
+        const int prg = i > 0 ? t.g[i - 1] : pg;
+        const uint32_t nxk = i + 1 < kWI ? t.k[i + 1] : nk;
+        const int nxg = i + 1 < kWI ? t.g[i + 1] : ng;
+        const bool gh = v && (kk == 0 || prg != t.g[i]);
+        const bool sh = v && (gh || prk != t.k[i]);
+        const bool nsh = kk + 1 >= A || nxg != t.g[i] || nxk != t.k[i];
+        t.valid |= (unsigned)v << i;
+        t.gh |= (unsigned)gh << i;
+        t.sh |= (unsigned)sh << i;
+        t.nsh |= (unsigned)nsh << i;
     }
 }
 
@@ -696,15 +703,10 @@ __global__ void __launch_bounds__(kThreads) k_split_count(SplitArgs a) {
         int base = tile * kWT;
         WarpTile t;
         wt_load<false>(a, A, base, t);
-        uint32_t surv = 0;
-        int sub = -1, grp = -1;
-#pragma unroll
-        for (int i = 0; i < kWI; ++i) {
-            int kk = base + 32 * i + (int)lane_id();
-            surv += (t.valid[i] && !(t.sh[i] && t.nsh[i])) ? 1u : 0u;
-            if (t.sh[i]) sub = kk;
-            if (t.gh[i]) grp = kk;
-        }
+        const int first = base + kWI * (int)lane_id();
+        uint32_t surv = __popc(t.valid & ~(t.sh & t.nsh));
+        int sub = t.sh ? first + 31 - __clz(t.sh) : -1;
+        int grp = t.gh ? first + 31 - __clz(t.gh) : -1;
         surv = warp_sum(surv);
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) {
@@ -827,59 +829,78 @@ __global__ void __launch_bounds__(kThreads) k_pscan_apply(SplitArgs a, const uin
 }
 
 __global__ void __launch_bounds__(kThreads, 5) k_split_apply(SplitArgs a) {
+    // a warp tile's survivors (from the front) and finished suffixes (from the
+    // back), staged so that both leave as coalesced rows
+    __shared__ int2 stage[kWarps][kWT];
     int A = *a.A;
     int ntiles = (A + kWT - 1) / kWT;
     int nwarps = gridDim.x * kWarps;
-    const unsigned ln = lane_id();
-    const unsigned lt_mask = (1u << ln) - 1u;
+    const int ln = (int)lane_id();
+    int2* st = stage[warp_id()];
+    const unsigned long long pol = l2_keep_policy();
     for (int tile = blockIdx.x * kWarps + (int)warp_id(); tile < ntiles; tile += nwarps) {
-        int base = tile * kWT;
+        const int base = tile * kWT;
         WarpTile t;
         wt_load<true>(a, A, base, t);
-        uint32_t dest = a.p_surv[tile];
-        int csub = a.p_sub[tile], cgrp = a.p_grp[tile];
+        const int first = base + kWI * ln;
+        const uint32_t dest = a.p_surv[tile];
+        // this lane's survivors, last subgroup head and last group head, and
+        // the exclusive values of the lanes before it
+        const unsigned alive = t.valid & ~(t.sh & t.nsh);
+        const int lsurv = __popc(alive);
+        const int lsub = t.sh ? first + 31 - __clz(t.sh) : -1;
+        const int lgrp = t.gh ? first + 31 - __clz(t.gh) : -1;
+        const int isurv = warp_incl_sum(lsurv);
+        const int lsing = __popc(t.valid) - lsurv;
+        const int ising = warp_incl_sum(lsing);
+        int atf = ising - lsing;  // this lane's first finished suffix, within the tile
+        int isub = warp_incl_max(lsub), igrp = warp_incl_max(lgrp);
+        int xsub = __shfl_up_sync(0xffffffffu, isub, 1), xgrp = __shfl_up_sync(0xffffffffu, igrp, 1);
+        if (ln == 0) xsub = xgrp = -1;
+        int ks = max(a.p_sub[tile], xsub), kg = max(a.p_grp[tile], xgrp);
+        int at = isurv - lsurv;  // this lane's first survivor, within the tile
 #pragma unroll
         for (int i = 0; i < kWI; ++i) {
-            int kk = base + 32 * i + (int)ln;
-            int ks = warp_incl_max(t.sh[i] ? kk : -1);
-            int kg = warp_incl_max(t.gh[i] ? kk : -1);
-            ks = max(ks, csub);
-            kg = max(kg, cgrp);
-            csub = __shfl_sync(0xffffffffu, ks, 31);
-            cgrp = __shfl_sync(0xffffffffu, kg, 31);
-            bool single = t.sh[i] && t.nsh[i];
-            bool surv = t.valid[i] && !single;
-            unsigned m = __ballot_sync(0xffffffffu, surv);
-            uint32_t d = dest + __popc(m & lt_mask);
-            dest += __popc(m);
-            if (t.valid[i]) {
-                int w = t.w[i];
-                int g = t.g[i];
-                int rank = g + (ks - kg);
-                if (a.write_rank == kRankAll || (a.write_rank == kRankChanged && rank != g))
-                    st_keep(a.R + w, rank, l2_keep_policy());
-                if (single) {
-                    a.SA[g + (kk - kg)] = w;
-                } else {
-                    __stcs(a.Wn + d, w);
-                    __stcs(a.Gn + d, rank);
-                }
+            if (!(t.valid >> i & 1u)) continue;
+            const int kk = first + i;
+            if (t.sh >> i & 1u) ks = kk;
+            if (t.gh >> i & 1u) kg = kk;
+            const int w = t.w[i], g = t.g[i];
+            const int rank = g + (ks - kg);
+            if (a.write_rank == kRankAll || (a.write_rank == kRankChanged && rank != g)) st_keep(a.R + w, rank, pol);
+            if (!(alive >> i & 1u)) {
+                st[kWT - 1 - atf] = make_int2(g + (kk - kg), w);
+                ++atf;
+                continue;
             }
-            // a surviving subgroup ends here: list it by class (one atomic per
-            // class and warp step for the descriptors, one for the slot count)
+            st[at] = make_int2(w, rank);
+            const uint32_t d = dest + (uint32_t)at;
+            ++at;
+            // a surviving subgroup longer than kSmallMax ends here: list it by class
             const int L = kk - ks + 1;
-            const bool ends = surv && t.nsh[i] && L > kSmallMax;
-            const int cls = !ends ? -1 : (L <= 64 ? 3 : (L <= a.medium_max ? 0 : (L <= kOT ? 1 : 2)));
-            const int2 dsc = make_int2((int)d - L + 1, L);
-            if (ends) {
+            if ((t.nsh >> i & 1u) && L > kSmallMax) {
+                const int cls = L <= 64 ? 3 : (L <= a.medium_max ? 0 : (L <= kOT ? 1 : 2));
                 const int ci = cls == 0 ? CNT_MED : (cls == 1 ? CNT_TILE : (cls == 2 ? CNT_LARGE : CNT_PAIR));
                 const int ce = cls == 0 ? CNT_MED_ELEMS
                                         : (cls == 1 ? CNT_TILE_ELEMS : (cls == 2 ? CNT_LARGE_ELEMS : CNT_PAIR_ELEMS));
                 int2* list = cls == 0 ? a.list_med : (cls == 1 ? a.list_tile : (cls == 2 ? a.list_large : a.list_rbc));
-                list[atomicAdd(&a.counters[ci], 1)] = dsc;
+                list[atomicAdd(&a.counters[ci], 1)] = make_int2((int)d - L + 1, L);
                 atomicAdd(&a.counters[ce], L);
             }
         }
+        __syncwarp();
+        const int tot = __shfl_sync(0xffffffffu, isurv, 31);
+        for (int j = ln; j < tot; j += 32) {
+            const int2 v = st[j];
+            __stcs(a.Wn + dest + j, v.x);
+            __stcs(a.Gn + dest + j, v.y);
+        }
+        const int fin = __shfl_sync(0xffffffffu, ising, 31);
+        for (int j = ln; j < fin; j += 32) {
+            const int2 v = st[kWT - 1 - j];
+            a.SA[v.x] = v.y;
+        }
+        __syncwarp();
     }
 }
 
