@@ -797,6 +797,48 @@ __global__ void __launch_bounds__(kThreads) k_pscan_top(SplitArgs a, uint32_t* _
     }
 }
 
+// Short rounds: one CTA scans all per-tile partials in place (what
+// k_pscan_reduce, k_pscan_top and k_pscan_apply do together).
+constexpr int kPscanSingleMax = 4096;  // warp tiles
+
+__global__ void __launch_bounds__(kThreads) k_pscan_single(SplitArgs a) {
+    __shared__ uint32_t shs[kWarps + 1];
+    __shared__ int shm[kWarps + 1];
+    const int n = (*a.A + kWT - 1) / kWT;
+    uint32_t carry = 0;
+    int c1 = -1, c2 = -1;
+    for (int base = 0; base < n; base += kThreads) {
+        const int i = base + threadIdx.x;
+        const bool ok = i < n;
+        const uint32_t v = ok ? a.p_surv[i] : 0u;
+        const int m1 = ok ? a.p_sub[i] : -1, m2 = ok ? a.p_grp[i] : -1;
+        uint32_t tot;
+        const uint32_t ex = block_excl_sum(v, shs, &tot);
+        int t1, t2;
+        const int e1 = block_excl_max(m1, shm, &t1);
+        const int e2 = block_excl_max(m2, shm, &t2);
+        if (ok) {
+            a.p_surv[i] = carry + ex;
+            a.p_sub[i] = max(c1, e1);
+            a.p_grp[i] = max(c2, e2);
+        }
+        carry += tot;
+        c1 = max(c1, t1);
+        c2 = max(c2, t2);
+    }
+    if (threadIdx.x == 0) {
+        *a.A_next = (int)carry;
+        a.counters[CNT_PAIR] = 0;
+        a.counters[CNT_PAIR_ELEMS] = 0;
+        a.counters[CNT_MED] = 0;
+        a.counters[CNT_TILE] = 0;
+        a.counters[CNT_LARGE] = 0;
+        a.counters[CNT_MED_ELEMS] = 0;
+        a.counters[CNT_TILE_ELEMS] = 0;
+        a.counters[CNT_LARGE_ELEMS] = 0;
+    }
+}
+
 __global__ void __launch_bounds__(kThreads) k_pscan_apply(SplitArgs a, const uint32_t* __restrict__ cs,
                                                           const int* __restrict__ cm1,
                                                           const int* __restrict__ cm2) {
@@ -1142,12 +1184,16 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
         long long tiles_n = (A + kWT - 1) / kWT;
         // count: key and group rank of every slot; 12 bytes of partials per tile
         QZ_LAUNCH(S, st, "k_split_count", 8 * A + 12 * tiles_n, k_split_count<<<grid, kThreads, 0, st>>>(a));
-        QZ_LAUNCH(S, st, "k_pscan_reduce", 12 * tiles_n,
-                  k_pscan_reduce<<<kScanGrid, kThreads, 0, st>>>(a, f.c_surv, f.c_sub, f.c_grp));
-        QZ_LAUNCH(S, st, "k_pscan_top", 24ll * kScanGrid,
-                  k_pscan_top<<<1, kThreads, 0, st>>>(a, f.c_surv, f.c_sub, f.c_grp, kScanGrid));
-        QZ_LAUNCH(S, st, "k_pscan_apply", 24 * tiles_n,
-                  k_pscan_apply<<<kScanGrid, kThreads, 0, st>>>(a, f.c_surv, f.c_sub, f.c_grp));
+        if (tiles_n <= kPscanSingleMax) {
+            QZ_LAUNCH(S, st, "k_pscan_single", 24 * tiles_n, k_pscan_single<<<1, kThreads, 0, st>>>(a));
+        } else {
+            QZ_LAUNCH(S, st, "k_pscan_reduce", 12 * tiles_n,
+                      k_pscan_reduce<<<kScanGrid, kThreads, 0, st>>>(a, f.c_surv, f.c_sub, f.c_grp));
+            QZ_LAUNCH(S, st, "k_pscan_top", 24ll * kScanGrid,
+                      k_pscan_top<<<1, kThreads, 0, st>>>(a, f.c_surv, f.c_sub, f.c_grp, kScanGrid));
+            QZ_LAUNCH(S, st, "k_pscan_apply", 24 * tiles_n,
+                      k_pscan_apply<<<kScanGrid, kThreads, 0, st>>>(a, f.c_surv, f.c_sub, f.c_grp));
+        }
         // apply: key, group, suffix in; ranks out per rank_mode; then the
         // suffix either leaves (SA) or is compacted (2 words); fixed up below
         QZ_LAUNCH(S, st, rank_mode == kRankNone ? "k_split_apply_first" : "k_split_apply", 12 * A + 12 * tiles_n,

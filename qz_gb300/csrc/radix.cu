@@ -158,6 +158,35 @@ __global__ void __launch_bounds__(kThreads) k_big_prep(const int2* __restrict__ 
     }
 }
 
+// One CTA plans the large-group sort when the list is short (every launch of
+// it counts): tiles and workspace offsets per group (exclusive scans of the
+// tile counts and lengths), the total tile count, and cleared pass masks.
+constexpr int kPlanMaxGroups = 32768;
+
+__global__ void __launch_bounds__(kThreads) k_big_plan(const int2* __restrict__ list, const int* __restrict__ d_count,
+                                                       uint32_t* __restrict__ tbase, uint32_t* __restrict__ wbase,
+                                                       uint32_t* __restrict__ gmask, int* __restrict__ total_tiles) {
+    __shared__ uint32_t sh[kWarps + 1];
+    const int cnt = *d_count;
+    uint32_t ct = 0, cw = 0;
+    for (int b0 = 0; b0 < cnt; b0 += kThreads) {
+        const int i = b0 + threadIdx.x;
+        const uint32_t len = i < cnt ? (uint32_t)list[i].y : 0u;
+        const uint32_t tl = (len + kOT - 1) / kOT;
+        uint32_t tt, tw;
+        const uint32_t et = block_excl_sum(tl, sh, &tt);
+        const uint32_t ew = block_excl_sum(len, sh, &tw);
+        if (i < cnt) {
+            tbase[i] = ct + et;
+            wbase[i] = cw + ew;
+            gmask[i] = 0;
+        }
+        ct += tt;
+        cw += tw;
+    }
+    if (threadIdx.x == 0) *total_tiles = (int)ct;
+}
+
 // largest s in [0, n) with tbase[s] <= tau
 __device__ __forceinline__ int big_seg_of_tile(const uint32_t* __restrict__ tbase, int n, uint32_t tau) {
     int lo = 0, hi = n - 1;
@@ -485,11 +514,16 @@ void sort_big_groups(Storage* S, const int2* list, const int* d_count, int host_
     FwdBuffers& f = S->f;
     int* cnt = S->counters;
     const int sms = S->sms;
-    QZ_LAUNCH(S, st, "k_big_prep", 20ll * host_count,
-              k_big_prep<<<grid_cap(host_count, kThreads, sms * 4), kThreads, 0, st>>>(list, d_count, f.ltc, f.llen,
-                                                                                      f.gmask));
-    scan_exclusive(S, f.ltc, f.ltbase, 0, d_count, (uint32_t*)(cnt + CNT_LTILES), st);
-    scan_exclusive(S, f.llen, f.lwbase, 0, d_count, nullptr, st);
+    if (host_count <= kPlanMaxGroups) {
+        QZ_LAUNCH(S, st, "k_big_plan", 20ll * host_count,
+                  k_big_plan<<<1, kThreads, 0, st>>>(list, d_count, f.ltbase, f.lwbase, f.gmask, cnt + CNT_LTILES));
+    } else {
+        QZ_LAUNCH(S, st, "k_big_prep", 20ll * host_count,
+                  k_big_prep<<<grid_cap(host_count, kThreads, sms * 4), kThreads, 0, st>>>(list, d_count, f.ltc,
+                                                                                          f.llen, f.gmask));
+        scan_exclusive(S, f.ltc, f.ltbase, 0, d_count, (uint32_t*)(cnt + CNT_LTILES), st);
+        scan_exclusive(S, f.llen, f.lwbase, 0, d_count, nullptr, st);
+    }
     BigArgs a{list, d_count, f.ltbase, f.lwbase, cnt + CNT_LTILES, f.gmask};
     BigBuffers bb{key, val, {f.wsk[0], f.wsk[1]}, {f.wsv[0], f.wsv[1]}};
     uint32_t* h4 = f.h4;
