@@ -322,6 +322,36 @@ def run_gpu(args, rank: int, world: int):
                 "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                 "alg_bytes_per_launch": int(per_launch_bytes), "launches_timed": top["launches"],
                 "traffic": (tr.get("bytes_per_launch") if isinstance(tr, dict) else tr)}
+        # the same kernel timed with the GPU to itself (a one-lane storage, one
+        # forward pass of the workload): its own rate, without the other lanes'
+        # kernels inside its event windows
+        if world == 1:
+            old = os.environ.get("QZGPU_LANES")
+            os.environ["QZGPU_LANES"] = "1"
+            try:
+                st1 = bwt.Storage(N, len(blocks))
+            finally:
+                if old is None:
+                    del os.environ["QZGPU_LANES"]
+                else:
+                    os.environ["QZGPU_LANES"] = old
+            for k, v in (tuned or {}).items():
+                st1.set_param(k, int(v))
+            st1.encode_device(sizes, d_T.data_ptr(), d_U.data_ptr(), sptr)
+            st1.profile(True, only=top["name"])
+            st1.profile_read(reset=True)
+            st1.encode_device(sizes, d_T.data_ptr(), d_U.data_ptr(), sptr)
+            torch.cuda.synchronize(dev)
+            p1 = st1.profile_read(reset=True)
+            st1.profile(False)
+            st1.close()
+            if p1 and p1[0]["launches"]:
+                b1 = p1[0]["alg_bytes"] / p1[0]["launches"]
+                s1 = p1[0]["ms"] / p1[0]["launches"] / 1e3
+                a1 = b1 / s1 / 1e9 if s1 > 0 else 0.0
+                roof["alone"] = {"achieved": round(a1, 1), "frac": round(a1 / peak, 4),
+                                 "launches": p1[0]["launches"],
+                                 "how": "one forward pass of the workload on a one-lane storage"}
 
     # ---- plain one-block-per-call path on the same device-resident inputs
     plain = None
