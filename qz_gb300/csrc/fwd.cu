@@ -440,28 +440,34 @@ __global__ void __launch_bounds__(kThreads) k_sort_straddle(const int* __restric
     }
 }
 
-// 65..512 slots: stable LSD radix sort by one warp in its share of shared
-// memory (key / suffix ping-pong buffers and 256 digit counters); lane l
-// holds slots it*32 + l, ranks within equal digits come from warp matches;
-// 8-bit digits that are equal across the whole group are skipped.
-constexpr size_t kMedWarpSmem = (size_t)kMedMax * 16 + 256 * 4;
+// 65..512 slots: stable LSD radix sort by one warp.  Lane l holds slots
+// it*32 + l in registers; each pass ranks them (warp matches, 256 digit
+// counters in shared memory), scatters (key, suffix) pairs into the warp's one
+// shared buffer and reads them back in the new order.  8-bit digits that are
+// equal across the whole group are skipped.
+constexpr size_t kMedWarpSmem = (size_t)kMedMax * 8 + 256 * 4;
 
 __device__ __forceinline__ void warp_radix_sort(uint32_t* __restrict__ key, int* __restrict__ W, int s, int len,
                                                 unsigned char* wsm) {
-    uint32_t* ks = reinterpret_cast<uint32_t*>(wsm);
-    uint32_t* kd = ks + kMedMax;
-    int* vs = reinterpret_cast<int*>(kd + kMedMax);
-    int* vd = vs + kMedMax;
-    uint32_t* cnt = reinterpret_cast<uint32_t*>(vd + kMedMax);
+    unsigned long long* buf = reinterpret_cast<unsigned long long*>(wsm);
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(buf + kMedMax);
     const int ln = (int)lane_id();
     const unsigned lt = (1u << ln) - 1u;
+    const int nit = (len + 31) >> 5;
+    uint32_t kr[kMedMax / 32];
+    int vr[kMedMax / 32];
     uint32_t kor = 0, kand = 0xffffffffu;
-    for (int j = ln; j < len; j += 32) {
-        uint32_t k = key[s + j];
-        ks[j] = k;
-        vs[j] = W[s + j];
-        kor |= k;
-        kand &= k;
+#pragma unroll
+    for (int it = 0; it < kMedMax / 32; ++it) {
+        const int i = it * 32 + ln;
+        kr[it] = 0;
+        vr[it] = 0;
+        if (it < nit && i < len) {
+            kr[it] = key[s + i];
+            vr[it] = W[s + i];
+            kor |= kr[it];
+            kand &= kr[it];
+        }
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
@@ -469,8 +475,6 @@ __device__ __forceinline__ void warp_radix_sort(uint32_t* __restrict__ key, int*
         kand &= __shfl_xor_sync(0xffffffffu, kand, d);
     }
     const uint32_t diff = kor ^ kand;
-    const int nit = (len + 31) >> 5;
-    __syncwarp();
     for (int pass = 0; pass < 4; ++pass) {
         const int sh = 8 * pass;
         if (((diff >> sh) & 255u) == 0) continue;
@@ -481,9 +485,8 @@ __device__ __forceinline__ void warp_radix_sort(uint32_t* __restrict__ key, int*
 #pragma unroll
         for (int it = 0; it < kMedMax / 32; ++it) {
             if (it < nit) {
-                const int i = it * 32 + ln;
-                const bool valid = i < len;
-                const unsigned dg = valid ? (ks[i] >> sh) & 255u : 256u;
+                const bool valid = it * 32 + ln < len;
+                const unsigned dg = valid ? (kr[it] >> sh) & 255u : 256u;
                 const unsigned peers = __match_any_sync(0xffffffffu, dg);
                 const unsigned before = __popc(peers & lt);
                 const uint32_t prev = valid ? cnt[dg] : 0u;
@@ -505,27 +508,30 @@ __device__ __forceinline__ void warp_radix_sort(uint32_t* __restrict__ key, int*
         __syncwarp();
 #pragma unroll
         for (int it = 0; it < kMedMax / 32; ++it) {
-            const int i = it * 32 + ln;
-            if (it < nit && i < len) {
-                const uint32_t k = ks[i];
-                const uint32_t p = cnt[(k >> sh) & 255u] + rk[it];
-                kd[p] = k;
-                vd[p] = vs[i];
+            if (it < nit && it * 32 + ln < len) {
+                const uint32_t p = cnt[(kr[it] >> sh) & 255u] + rk[it];
+                buf[p] = ((unsigned long long)kr[it] << 32) | (uint32_t)vr[it];
             }
         }
         __syncwarp();
-        uint32_t* tk = ks;
-        ks = kd;
-        kd = tk;
-        int* tv = vs;
-        vs = vd;
-        vd = tv;
+#pragma unroll
+        for (int it = 0; it < kMedMax / 32; ++it) {
+            if (it < nit && it * 32 + ln < len) {
+                const unsigned long long v = buf[it * 32 + ln];
+                kr[it] = (uint32_t)(v >> 32);
+                vr[it] = (int)(uint32_t)v;
+            }
+        }
+        __syncwarp();
     }
-    for (int j = ln; j < len; j += 32) {
-        key[s + j] = ks[j];
-        W[s + j] = vs[j];
+#pragma unroll
+    for (int it = 0; it < kMedMax / 32; ++it) {
+        const int i = it * 32 + ln;
+        if (it < nit && i < len) {
+            key[s + i] = kr[it];
+            W[s + i] = vr[it];
+        }
     }
-    __syncwarp();
 }
 
 // Groups of 17..64 slots, one warp per listed group: each slot ranks itself by
@@ -575,7 +581,7 @@ __global__ void __launch_bounds__(kThreads) k_sort_rbc(const int2* __restrict__ 
 }
 
 // Groups of 65..512 slots, one warp per listed group: warp_radix_sort.
-__global__ void __launch_bounds__(kThreads) k_sort_medium(const int2* __restrict__ list,
+__global__ void __launch_bounds__(kThreads, 3) k_sort_medium(const int2* __restrict__ list,
                                                           const int* __restrict__ d_count,
                                                           uint32_t* __restrict__ key, int* __restrict__ W) {
     extern __shared__ __align__(16) unsigned char msm[];

@@ -245,3 +245,16 @@ def test_batch_out_buffers_reused(gpu):
             assert all((x == y).all() for x, y in zip(back, blocks))
         with pytest.raises(native.QzGpuError):
             st.encode_batch(blocks, out=outs[:2])
+
+
+@pytest.mark.parametrize("kind", ["header", "quality"])
+def test_large_repetitive_blocks(gpu, oracle, kind):
+    # multi-megabyte header / quality blocks: large groups over several rounds,
+    # radix passes skipped where a group's digit is constant
+    t = synth.header_stream(120_000, seed=97) if kind == "header" else synth.quality_stream(40_000, seed=98)
+    _check_block(oracle, t)
+    with bwt.Storage(2 * len(t), 2) as st:
+        us, idx = st.encode_batch([t, t[: len(t) // 2]])
+        ous, oidx = oracle.bwt_encode_batch([t, t[: len(t) // 2]])
+        assert idx == list(oidx)
+        assert all((u == ou).all() for u, ou in zip(us, ous))
