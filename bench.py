@@ -46,6 +46,9 @@ def make_workload(name: str, reads: int):
     elif name == "uneven":
         blocks = synth.uneven_blocks(256)
         desc = "256 blocks, sizes log-uniform 1 KB-25 MiB, 50% DNA / 30% quality / 20% header"
+    elif name == "ultra":
+        blocks = [("seq", synth.ultra_block())]
+        desc = "one 750 MiB ultra-mode sequence block (150 bp reads, 50 Mbp genome)"
     elif name == "repeat":
         blocks = synth.repeat_blocks()
         desc = "repeat-rich: 250 bp reads at 30x over 1 Mbp with 20% tandem repeats, one single-byte and one period-3 block"
@@ -562,7 +565,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="chunk", choices=["chunk", "plain", "uneven", "repeat", "serve"])
+    ap.add_argument("--config", default="chunk", choices=["chunk", "plain", "uneven", "repeat", "ultra", "serve"])
     ap.add_argument("--requests", type=int, default=300, help="serve: requests per load point")
     ap.add_argument("--slots", type=int, default=4, help="serve: device slots (bounded by free HBM)")
     ap.add_argument("--reads", type=int, default=2_500_000)

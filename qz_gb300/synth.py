@@ -185,6 +185,15 @@ def chunk_blocks(nreads: int = 2_500_000) -> list[tuple[str, np.ndarray]]:
     return out
 
 
+def ultra_block(nbytes: int = 750 * 1024 * 1024, seed: int = 8) -> np.ndarray:
+    """One ultra-mode sequence block (qz's reorder levels use BSC blocks up to
+    750 MiB, ultra.rs:44-55): 150 bp reads from a 50 Mbp genome (seed 8),
+    truncated to `nbytes`."""
+    g = uniform_genome(50_000_000, seed=seed)
+    reads = nbytes // READ_LEN + 1
+    return sample_reads(g, reads, seed=seed + 1)[:nbytes]
+
+
 def _source_streams(max_len: int, seed: int) -> dict[str, np.ndarray]:
     reads = max_len // READ_LEN + 1
     g = uniform_genome(5_000_000, seed=1)

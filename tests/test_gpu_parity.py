@@ -258,3 +258,32 @@ def test_large_repetitive_blocks(gpu, oracle, kind):
         ous, oidx = oracle.bwt_encode_batch([t, t[: len(t) // 2]])
         assert idx == list(oidx)
         assert all((u == ou).all() for u, ou in zip(us, ous))
+
+
+def test_block_above_lane_size(gpu, oracle):
+    # an 80 MB block is larger than a lane's 64 MiB sub-batch: it runs alone on
+    # the full-capacity lane, next to small blocks on the others
+    g = synth.uniform_genome(2_000_000, seed=99)
+    big = synth.sample_reads(g, 80_000_000 // 150, seed=100)
+    small = [synth.quality_stream(3000, seed=101), synth.header_stream(4000, seed=102)]
+    blocks = [small[0], big, small[1]]
+    with bwt.Storage(sum(len(b) for b in blocks), len(blocks)) as st:
+        us, idx = st.encode_batch(blocks)
+        ous, oidx = oracle.bwt_encode_batch(blocks)
+        assert idx == list(oidx)
+        assert all((u == ou).all() for u, ou in zip(us, ous))
+        back = st.decode_batch(us, idx)
+        assert all((x == y).all() for x, y in zip(back, blocks))
+
+
+def test_ultra_block_round_trip(gpu):
+    # a 300 MiB block (qz's reorder levels use blocks up to 750 MiB): the
+    # inverse of the forward is the input (size-independent property; the
+    # oracle parity of the same path is checked at 80 MB above)
+    t = synth.ultra_block(300 << 20)
+    with bwt.Storage(len(t), 1) as st:
+        (u,), (idx,) = st.encode_batch([t])
+        assert 1 <= idx <= len(t)
+        assert np.bincount(u, minlength=256).tolist() == np.bincount(t, minlength=256).tolist()
+        (back,) = st.decode_batch([u], [idx])
+        assert (back == t).all()
