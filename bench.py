@@ -559,13 +559,69 @@ def run_serve(args, rank: int, world: int):
         print(json.dumps(line), flush=True)
 
 
+def run_streams(args, rank: int):
+    """Stream building on the device: one qz chunk's FASTQ text (2.5M x 150 bp
+    reads) -> header / sequence / quality streams through qzgpu_fastq_streams
+    (host buffers in and out, pinned and reused; copies inside the timed
+    region).  CPU side: the Python oracle on a bounded sample of records."""
+    import torch
+
+    from qz_gb300 import bwt
+    from qz_gb300 import streams as G
+
+    if rank != 0:
+        return
+    text = synth_chunk_fastq(args.reads)
+    n = len(text)
+    bwt.init()
+    pin = torch.empty(n, dtype=torch.uint8, pin_memory=True).numpy()
+    pin[:] = text
+    h, s, q, info = G.fastq_streams(pin)
+    out = tuple(torch.empty(max(len(x), 1), dtype=torch.uint8, pin_memory=True).numpy()[: len(x)] for x in (h, s, q))
+    for _ in range(args.warmup):
+        G.fastq_streams(pin, out=out)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        G.fastq_streams(pin, out=out)
+    dt = (time.perf_counter() - t0) / args.steps
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import streams as S
+
+        k = min(len(text), 200_000 * 360)
+        sample = bytes(text[:k])
+        cut = sample.rfind(b"\n@SIM") + 1  # whole records only
+        t1 = time.perf_counter()
+        S.fastq_streams(sample[:cut])
+        c = time.perf_counter() - t1
+        cpu = {"value": round(cut / c / 1e6, 3), "unit": "MB/s", "cores": 1, "kind": "port",
+               "sample": f"first {cut} bytes of the text; Python oracle, not qz's Rust"}
+    line = {"metric": "FASTQ -> qz streams MB/s (FASTQ bytes) on 1 GB300", "value": round(n / dt / 1e6, 3),
+            "unit": "MB/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u8", "data": "synthetic (the chunk workload's reads as FASTQ text)",
+            "config": {"workload": f"one qz chunk as FASTQ: {args.reads} x 150 bp reads, {n} bytes",
+                       "path": "qzgpu_fastq_streams, pinned host buffers reused"},
+            "streams": {k: v for k, v in info.items()}, "e2e": {"value": round(n / dt / 1e6, 3), "unit": "MB/s",
+                                                               "h2d_bytes_per_step": n,
+                                                               "d2h_bytes_per_step": len(h) + len(s) + len(q)},
+            "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+
+
+def synth_chunk_fastq(reads: int):
+    from qz_gb300 import synth
+
+    return synth.chunk_fastq(reads)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="chunk", choices=["chunk", "plain", "uneven", "repeat", "ultra", "serve"])
+    ap.add_argument("--config", default="chunk", choices=["chunk", "plain", "uneven", "repeat", "ultra", "serve", "streams"])
     ap.add_argument("--requests", type=int, default=300, help="serve: requests per load point")
     ap.add_argument("--slots", type=int, default=4, help="serve: device slots (bounded by free HBM)")
     ap.add_argument("--reads", type=int, default=2_500_000)
@@ -583,6 +639,8 @@ def main():
         run_reference(args, rank)
     elif args.config == "serve":
         run_serve(args, rank, world)
+    elif args.config == "streams":
+        run_streams(args, rank)
     else:
         run_gpu(args, rank, world)
 

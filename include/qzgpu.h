@@ -236,6 +236,42 @@ int qzgpu_server_destroy(qzgpu_server *server);
  * negative code. */
 int qzgpu_bwt_decode_noalloc(const unsigned char *d_U, unsigned char *d_T, int n, int index, void *stream);
 
+/* ------------------------------------------------------------------------- */
+/* Stream building on the device (the step before the block sorter).         */
+/* ------------------------------------------------------------------------- */
+
+/* Replaces records_to_streams (crates/qz-lib/src/compression/mod.rs:270-325)
+ * on qz's default lossless BSC path (quality mode lossless, binning none:
+ * 7 bits per quality, columnar.rs:16-36 and 104-134; no sequence hints, delta
+ * or reverse-complement canonicalisation), together with the FASTQ reader that
+ * feeds it (FastqReader::next, io/fastq.rs:135-200) and detect_const_lengths
+ * (mod.rs:329-354): FASTQ text in, qz's three streams out.
+ *
+ *   header stream    [varint(len(id))][id]          (id: the '@' line)
+ *   sequence stream  [varint(len) if lengths vary][bases]
+ *   quality stream   [varint(len) if lengths vary][qualities, 7 bits each,
+ *                    LSB first, min(max(q - 33, 0), 127), per read]
+ *
+ * Records follow the reader: four lines each, trailing '\r' trimmed, the third
+ * line must start with '+', sequence and quality lengths must match, and an
+ * input that ends inside a record is an error.  Returns 0,
+ * QZGPU_DATA_CORRUPT for malformed input (info->error_record = the record the
+ * reader fails on), or QZGPU_BAD_PARAMETER when an output capacity is below
+ * the size in info (call with null outputs and zero capacities to size them).
+ * Text up to 2 GiB - 1.  No counterpart in libbsc. */
+typedef struct qzgpu_streams_info {
+    long long records;
+    long long header_bytes;
+    long long seq_bytes;
+    long long qual_bytes;
+    int const_seq_len;   /* 0: lengths vary (length varints written) */
+    int const_qual_len;
+    long long error_record; /* -1 when the input is well formed */
+} qzgpu_streams_info;
+int qzgpu_fastq_streams(const unsigned char *fastq, long long n, unsigned char *header_out, long long header_cap,
+                        unsigned char *seq_out, long long seq_cap, unsigned char *qual_out, long long qual_cap,
+                        qzgpu_streams_info *info);
+
 #ifdef __cplusplus
 }
 #endif

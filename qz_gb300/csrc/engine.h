@@ -211,6 +211,8 @@ int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t*
                 cudaStream_t st);
 
 int map_cuda_error(cudaError_t e);
+// The library's device (initialised on first use) and its SM count.
+int device_info(int* device, int* sms);
 
 // Host-buffer batch calls on a storage the caller holds (copies in, runs,
 // copies out, synchronises the storage's stream).

@@ -428,6 +428,14 @@ int decode_host(Storage* S, int nb, const unsigned char* const* U, unsigned char
     return map_cuda_error(e);
 }
 
+int device_info(int* device, int* sms) {
+    int rc = ensure_init();
+    if (rc) return rc;
+    *device = G().device;
+    *sms = G().sms;
+    return QZGPU_NO_ERROR;
+}
+
 }  // namespace qz
 
 namespace {

@@ -49,6 +49,13 @@ class KernelTime(ctypes.Structure):
                 ("alg_bytes", ctypes.c_longlong)]
 
 
+class StreamsInfo(ctypes.Structure):
+    _fields_ = [("records", ctypes.c_longlong), ("header_bytes", ctypes.c_longlong),
+                ("seq_bytes", ctypes.c_longlong), ("qual_bytes", ctypes.c_longlong),
+                ("const_seq_len", ctypes.c_int), ("const_qual_len", ctypes.c_int),
+                ("error_record", ctypes.c_longlong)]
+
+
 _u8p = ctypes.POINTER(ctypes.c_uint8)
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _vp = ctypes.c_void_p
@@ -72,6 +79,8 @@ SIGNATURES = {
     "qzgpu_storage_last_stats": (ctypes.c_int, [_vp, ctypes.POINTER(Stats)]),
     "qzgpu_storage_profile": (ctypes.c_int, [_vp, ctypes.c_int]),
     "qzgpu_storage_profile_only": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+    "qzgpu_fastq_streams": (ctypes.c_int, [_u8p, ctypes.c_longlong, _u8p, ctypes.c_longlong, _u8p, ctypes.c_longlong,
+                                           _u8p, ctypes.c_longlong, _vp]),
     "qzgpu_storage_set_param": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_longlong]),
     "qzgpu_storage_get_param": (ctypes.c_longlong, [_vp, ctypes.c_char_p]),
     "qzgpu_bwt_decode_noalloc": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),

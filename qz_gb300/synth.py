@@ -83,13 +83,9 @@ def sample_reads(genome: np.ndarray, nreads: int, seed: int, read_len: int = REA
     return out
 
 
-def quality_stream(nreads: int, seed: int, read_len: int = READ_LEN, chunk: int = 200_000) -> np.ndarray:
-    """Phred values {2,12,23,37} from a per-read Markov chain whose
-    stay-probability falls linearly from 0.95 to 0.80 along the read, packed
-    7 bits per value LSB-first per read (columnar.rs:104-134)."""
+def _quality_chunks(nreads: int, seed: int, read_len: int, chunk: int):
+    """(first read, Phred values of up to `chunk` reads) from the quality model."""
     rng = np.random.default_rng(seed)
-    per_read = (read_len * 7 + 7) // 8
-    out = np.empty(nreads * per_read, dtype=np.uint8)
     stay = 0.95 - 0.15 * np.arange(read_len) / max(read_len - 1, 1)
     init_p = np.array([0.05, 0.10, 0.25, 0.60])
     for lo in range(0, nreads, chunk):
@@ -102,6 +98,25 @@ def quality_stream(nreads: int, seed: int, read_len: int = READ_LEN, chunk: int 
                 step = rng.integers(1, 4, m)
                 state = np.where(move, (state + step) % 4, state)
             q[:, t] = QUAL_VALUES[state]
+        yield lo, q
+
+
+def quality_values(nreads: int, seed: int, read_len: int = READ_LEN, chunk: int = 200_000) -> np.ndarray:
+    """Phred values (reads x read_len) of the quality model below."""
+    out = np.empty((nreads, read_len), dtype=np.uint8)
+    for lo, q in _quality_chunks(nreads, seed, read_len, chunk):
+        out[lo:lo + len(q)] = q
+    return out
+
+
+def quality_stream(nreads: int, seed: int, read_len: int = READ_LEN, chunk: int = 200_000) -> np.ndarray:
+    """Phred values {2,12,23,37} from a per-read Markov chain whose
+    stay-probability falls linearly from 0.95 to 0.80 along the read, packed
+    7 bits per value LSB-first per read (columnar.rs:104-134)."""
+    per_read = (read_len * 7 + 7) // 8
+    out = np.empty(nreads * per_read, dtype=np.uint8)
+    for lo, q in _quality_chunks(nreads, seed, read_len, chunk):
+        m = len(q)
         bits = ((q[:, :, None] >> np.arange(7, dtype=np.uint8)) & 1).reshape(m, read_len * 7)
         pad = per_read * 8 - read_len * 7
         if pad:
@@ -119,11 +134,10 @@ def _varint(v: int) -> bytes:
     return bytes(b)
 
 
-def header_stream(nreads: int, seed: int) -> np.ndarray:
+def header_ids(nreads: int, seed: int) -> list[bytes]:
     """Illumina-style ids '@SIM:1:FC01:<lane>:<tile>:<x>:<y> 1:N:0:<8-mer>',
     reads laid out lane by lane and tile by tile with x and y increasing within
-    each tile; one sample index per lane with rare single-base errors.  Stream
-    layout ``[varint(len)][id]`` (mod.rs:291-292)."""
+    each tile; one sample index per lane with rare single-base errors."""
     rng = np.random.default_rng(seed)
     lanes, tiles = 4, 2624 - 1101 + 1
     cells = lanes * tiles
@@ -142,7 +156,7 @@ def header_stream(nreads: int, seed: int) -> np.ndarray:
     err = rng.random(nreads) < 0.005
     err_pos = rng.integers(0, 8, nreads)
     err_base = rng.integers(0, 4, nreads)
-    parts = []
+    ids = []
     for r in range(nreads):
         c = int(cell_of[r])
         lane, tile = c // tiles, 1101 + c % tiles
@@ -151,10 +165,58 @@ def header_stream(nreads: int, seed: int) -> np.ndarray:
             b = bytearray(idx)
             b[err_pos[r]] = b"ACGT"[err_base[r]]
             idx = bytes(b)
-        s = b"@SIM:1:FC01:%d:%d:%d:%d 1:N:0:%s" % (lane + 1, tile, xs[r], ys[r], idx)
+        ids.append(b"@SIM:1:FC01:%d:%d:%d:%d 1:N:0:%s" % (lane + 1, tile, xs[r], ys[r], idx))
+    return ids
+
+
+def header_stream(nreads: int, seed: int) -> np.ndarray:
+    """header_ids laid out as qz's header stream ``[varint(len)][id]``
+    (mod.rs:291-292)."""
+    parts = []
+    for s in header_ids(nreads, seed):
         parts.append(_varint(len(s)))
         parts.append(s)
     return np.frombuffer(b"".join(parts), dtype=np.uint8).copy()
+
+
+def fastq_text(ids: list[bytes], seqs: np.ndarray, quals: np.ndarray, chunk: int = 100_000) -> np.ndarray:
+    """FASTQ text ('\n' line ends) of reads with one length: id line, bases,
+    '+', Phred+33 qualities."""
+    n, L = seqs.shape
+    id_lens = np.fromiter((len(i) for i in ids), dtype=np.int64, count=n)
+    rec_len = id_lens + 2 * L + 5  # id, bases, "+", qualities, each with its newline
+    off = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(rec_len, out=off[1:])
+    out = np.empty(int(off[-1]), dtype=np.uint8)
+    ar = np.arange(L, dtype=np.int64)
+    for lo in range(0, n, chunk):
+        hi = min(n, lo + chunk)
+        ic = np.frombuffer(b"".join(ids[lo:hi]), dtype=np.uint8)
+        il = id_lens[lo:hi]
+        starts = off[lo:hi]
+        ioff = np.zeros(hi - lo, dtype=np.int64)
+        np.cumsum(il[:-1], out=ioff[1:])
+        out[np.repeat(starts - ioff, il) + np.arange(ic.size)] = ic
+        nl = starts + il
+        out[nl] = 10
+        sq = nl + 1
+        out[sq[:, None] + ar] = seqs[lo:hi]
+        out[sq + L] = 10
+        out[sq + L + 1] = ord("+")
+        out[sq + L + 2] = 10
+        qs = sq + L + 3
+        out[qs[:, None] + ar] = quals[lo:hi] + 33
+        out[qs + L] = 10
+    return out
+
+
+def chunk_fastq(nreads: int = 2_500_000) -> np.ndarray:
+    """The FASTQ text whose three qz streams are chunk_blocks' streams (same
+    genome, reads, qualities and ids; seeds 1-4)."""
+    g = uniform_genome(5_000_000, seed=1)
+    seq = sample_reads(g, nreads, seed=2).reshape(nreads, READ_LEN)
+    qual = quality_values(nreads, seed=3)
+    return fastq_text(header_ids(nreads, seed=4), seq, qual)
 
 
 def cut_blocks(stream: np.ndarray, block_bytes: int = BLOCK_BYTES) -> list[np.ndarray]:
