@@ -31,15 +31,40 @@ __device__ __forceinline__ int vlen(uint32_t v) {
     return v < (1u << 7) ? 1 : v < (1u << 14) ? 2 : v < (1u << 21) ? 3 : v < (1u << 28) ? 4 : 5;
 }
 
+// Newlines among the 256 bytes a thread owns (16-byte loads when the run is
+// inside the text; the text copy is 16-byte aligned).
+__device__ __forceinline__ uint32_t nl_bits16(uint4 v) {
+    // one bit per byte equal to '\n', in byte order
+    uint32_t m = 0;
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+#pragma unroll
+        for (int b = 0; b < 4; ++b) m |= (uint32_t)(((w[q] >> (8 * b)) & 0xffu) == '\n') << (4 * q + b);
+    }
+    return m;
+}
+
+__device__ __forceinline__ uint32_t count_nl(const uint8_t* __restrict__ text, long long n, long long base) {
+    uint32_t c = 0;
+    if (base + kStPerThread <= n) {
+        const uint4* p = reinterpret_cast<const uint4*>(text + base);
+#pragma unroll 4
+        for (int k = 0; k < kStPerThread / 16; ++k) c += __popc(nl_bits16(__ldg(p + k)));
+    } else {
+        for (int k = 0; k < kStPerThread; ++k) {
+            const long long x = base + k;
+            if (x < n) c += text[x] == '\n';
+        }
+    }
+    return c;
+}
+
 __global__ void __launch_bounds__(kThreads) k_nl_count(const uint8_t* __restrict__ text, long long n,
                                                        uint32_t* __restrict__ cnt) {
     __shared__ uint32_t sh[kWarps + 1];
     const long long base = (long long)blockIdx.x * kStTile + (long long)threadIdx.x * kStPerThread;
-    uint32_t c = 0;
-    for (int k = 0; k < kStPerThread; ++k) {
-        const long long x = base + k;
-        if (x < n) c += text[x] == '\n';
-    }
+    const uint32_t c = count_nl(text, n, base);
     uint32_t tot;
     block_excl_sum(c, sh, &tot);
     if (threadIdx.x == 0) cnt[blockIdx.x] = tot;
@@ -49,18 +74,23 @@ __global__ void __launch_bounds__(kThreads) k_nl_write(const uint8_t* __restrict
                                                        const uint32_t* __restrict__ tbase, int* __restrict__ line_end) {
     __shared__ uint32_t sh[kWarps + 1];
     const long long base = (long long)blockIdx.x * kStTile + (long long)threadIdx.x * kStPerThread;
-    uint32_t c = 0;
-    for (int k = 0; k < kStPerThread; ++k) {
-        const long long x = base + k;
-        if (x < n) c += text[x] == '\n';
-    }
+    const uint32_t c = count_nl(text, n, base);
     uint32_t tot;
     uint32_t at = tbase[blockIdx.x] + block_excl_sum(c, sh, &tot);
-    for (int k = 0; k < kStPerThread && c; ++k) {
-        const long long x = base + k;
-        if (x < n && text[x] == '\n') {
-            line_end[at++] = (int)x;
-            --c;
+    if (!c) return;
+    if (base + kStPerThread <= n) {
+        const uint4* p = reinterpret_cast<const uint4*>(text + base);
+        for (int k = 0; k < kStPerThread / 16; ++k) {
+            uint32_t m = nl_bits16(__ldg(p + k));
+            while (m) {
+                line_end[at++] = (int)(base + 16 * k + __ffs(m) - 1);
+                m &= m - 1;
+            }
+        }
+    } else {
+        for (int k = 0; k < kStPerThread; ++k) {
+            const long long x = base + k;
+            if (x < n && text[x] == '\n') line_end[at++] = (int)x;
         }
     }
 }
