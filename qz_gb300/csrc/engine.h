@@ -19,7 +19,7 @@
 namespace qz {
 
 // Segment classes of the per-round sort (by group length).
-constexpr int kSmallMax = 16;    // one thread, register bitonic network
+constexpr int kSmallMax = 16;    // longest group sorted by rank counting in a warp window
 constexpr int kMedMax = 512;     // one warp sorts a group of up to kMedMax slots
 constexpr int kOT = 4096;        // one CTA sorts a group of up to kOT slots; longer: onesweep tiles
 constexpr int kInitTile = 4096;  // text positions per tile of the per-block passes
@@ -32,7 +32,6 @@ enum Counter {
     CNT_MED = 2,     // descriptor counts of the listed classes
     CNT_LARGE = 3,
     CNT_LTILES = 4,  // tiles of the large-group radix sort
-    CNT_LHIST = 5,   // histogram entries of the large-group radix sort (256 per tile)
     CNT_ACTIVE_ALT = 6,
     CNT_MED_ELEMS = 8,  // slots covered by each listed class
     CNT_TILE = 10,
@@ -57,7 +56,7 @@ struct FwdBuffers {
     int2* list_tile;   // groups of 513..4096 slots
     int2* list_large;  // groups of more than 4096 slots
     uint8_t* straddle;  // per 32-slot window: a small group may cross its right boundary
-    uint32_t* h4;      // large groups: digit counts of all four passes
+    uint32_t* h4;      // large groups: digit counts of the four passes -> bases / pass-0 cursors
     unsigned long long* status64;  // look-back status per (tile, digit)
     uint32_t* gmask;   // large: per group, the passes whose digit is not constant
     uint32_t* ltc;     // large: tiles per group -> tile base

@@ -24,10 +24,11 @@
 // Groups are kept in a compact work list in SA order (slot arrays W =
 // suffix, G = group rank); a slot's SA position is G plus its offset in the
 // group.  Per round each group is sorted by the kernel of its size class:
-// <= 16 slots in registers (found from G, no list), <= 4096 in shared memory,
-// larger ones by a segmented LSD radix sort (8-bit digits, warp match-based
-// stable ranking, shared-memory staged scatter).  The secondary-key gather is
-// fused into the sorts.
+// <= 16 slots by rank counting in warp windows during the key gather (found
+// from G, no list), 17..64 by rank counting in one warp, 65..512 by a warp
+// radix sort, <= 4096 in one CTA's shared memory, larger ones by a segmented
+// LSD radix sort over the whole GPU (radix.cu).  Round 0 gathers text keys
+// (R holds them until round 0's split), so the initial split writes no ranks.
 #include "engine.h"
 #include "radix.cuh"
 #include "scan.cuh"

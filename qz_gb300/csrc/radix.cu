@@ -1,14 +1,19 @@
 // Segmented sorts of (32-bit key, 32-bit value) pairs in compact slot space
 // for groups longer than a warp can sort (sm_103a, integer only).
 //
-//   * groups of kTileMin..kOT slots: one CTA sorts the whole group in shared
-//     memory, four 8-bit LSD passes, reading and writing global memory once;
-//   * longer groups: one stable 8-bit LSD pass per launch over 4096-slot
-//     tiles ("onesweep"): per-group digit totals for all four passes come from
-//     one histogram kernel; each tile takes a ticket in order, publishes its
-//     digit counts, and looks back over the tiles before it in the same group
-//     for its exclusive prefix (decoupled look-back), then scatters through
-//     shared memory so that each digit's run leaves as coalesced writes.
+//   * groups of up to kOT slots: one CTA sorts the whole group in shared
+//     memory (8-bit LSD passes, digits constant across the group skipped),
+//     reading and writing global memory once;
+//   * longer groups: one 8-bit LSD pass per launch over 4096-slot tiles
+//     ("onesweep").  One histogram kernel gives each group's digit totals for
+//     all four passes and marks the passes whose digit is not constant in the
+//     group; the group runs only those.  Pass 0 needs no stability (equal keys
+//     may leave in any order): tiles rank with shared atomics and reserve their
+//     output with one atomic per digit on the group's cursor.  The later passes
+//     are stable: each tile takes a ticket in order, publishes its digit
+//     counts, and looks back over the tiles before it in the same group for
+//     its exclusive prefix (decoupled look-back), then scatters through shared
+//     memory so that each digit's run leaves as coalesced writes.
 //
 // Look-back waits are bounded: a tile only waits on tiles that took earlier
 // tickets, which publish their counts before they wait themselves; a wait that
