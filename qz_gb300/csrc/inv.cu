@@ -40,9 +40,12 @@ struct InvArgs {
     DevStatus* st;
 };
 
+// Per-tile symbol counts (order-independent): per-warp shared counters with
+// atomics, all of the tile's bytes loaded first.
 __global__ void __launch_bounds__(kThreads) k_inv_up(InvArgs a, uint32_t* __restrict__ hist) {
-    __shared__ uint32_t h[256];
-    h[threadIdx.x] = 0;
+    __shared__ uint32_t h[kWarps][256];
+#pragma unroll
+    for (int q = 0; q < kWarps; ++q) h[q][threadIdx.x] = 0;
     __syncthreads();
     int2 tl = a.tiles[blockIdx.x];
     int b = tl.x, s0 = tl.y;
@@ -57,13 +60,13 @@ __global__ void __launch_bounds__(kThreads) k_inv_up(InvArgs a, uint32_t* __rest
         cu[it] = x < end ? (unsigned)__ldg(a.U + x) : 256u;
     }
 #pragma unroll
-    for (int it = 0; it < kInitTile / kThreads; ++it) {
-        unsigned c = cu[it];
-        unsigned peers = __match_any_sync(0xffffffffu, c);
-        if (c < 256u && lane_id() == (unsigned)(__ffs(peers) - 1)) atomicAdd(&h[c], __popc(peers));
-    }
+    for (int it = 0; it < kInitTile / kThreads; ++it)
+        if (cu[it] < 256u) atomicAdd(&h[warp_id()][cu[it]], 1u);
     __syncthreads();
-    hist[(size_t)256 * a.tbase[b] + (size_t)threadIdx.x * m + j] = h[threadIdx.x];
+    uint32_t v = 0;
+#pragma unroll
+    for (int q = 0; q < kWarps; ++q) v += h[q][threadIdx.x];
+    hist[(size_t)256 * a.tbase[b] + (size_t)threadIdx.x * m + j] = v;
 }
 
 __global__ void __launch_bounds__(kThreads) k_inv_down(InvArgs a, const uint32_t* __restrict__ hist) {
