@@ -147,6 +147,9 @@ int qzgpu_storage_round_counts(const qzgpu_storage *storage, long long *active, 
  *   "tile_ctas_per_sm"                CTAs per SM of the one-CTA group sort (1..3)
  *   "medium_max"                      longest group sorted by one warp (64..512)
  *   "ruler_stride_log2"               inverse: a ruler every 2^v rows (3..12)
+ *   "lookback_test"                   1: failure-detection test (forward calls fail with
+ *                                     QZGPU_TIMEOUT through a bounded look-back wait that
+ *                                     runs out; no GPU fault); 0: off (default)
  * get_param also answers "lanes".  Returns 0 / the value, or QZGPU_BAD_PARAMETER
  * for an unknown name or an out-of-range value.  No counterpart in libbsc. */
 int qzgpu_storage_set_param(qzgpu_storage *storage, const char *name, long long value);

@@ -26,6 +26,13 @@ __device__ __forceinline__ void report(DevStatus* st, int code, int where, long 
     }
 }
 
+// True once any kernel has reported a problem: the kernels whose stores are
+// addressed by data that an earlier failure may have left inconsistent (suffix
+// indexes, digit positions) return at entry instead.
+__device__ __forceinline__ bool failed(const DevStatus* st) {
+    return *reinterpret_cast<const volatile int*>(&st->error) != 0;
+}
+
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 __device__ __forceinline__ unsigned warp_id() { return threadIdx.x >> 5; }
 

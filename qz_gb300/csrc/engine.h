@@ -86,6 +86,10 @@ struct Tune {
     int tile_ctas_per_sm = 3;  // CTAs of the one-CTA group sort
     int medium_max = kMedMax;  // longest group sorted by one warp (64..512)
     int ruler_log2 = 5;        // inverse: a ruler every 2^ruler_log2 rows (3..12)
+    // failure-detection test: in the first stable radix pass the second tile
+    // of every group publishes nothing and look-back waits give up after 4096
+    // polls, so the tiles after it report QZGPU_TIMEOUT (no GPU fault)
+    int lookback_test = 0;
 };
 
 struct Storage {

@@ -636,6 +636,7 @@ struct SplitArgs {
     int* p_grp;
     int write_rank;    // kRankNone / kRankChanged / kRankAll
     int medium_max;    // longest group listed for the one-warp sort
+    const DevStatus* st;
 };
 
 // Lane l of a warp tile holds the 8 consecutive slots base + 8l .. base + 8l + 7,
@@ -881,6 +882,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_split_apply(SplitArgs a) {
     // a warp tile's survivors (from the front) and finished suffixes (from the
     // back), staged so that both leave as coalesced rows
     __shared__ int2 stage[kWarps][kWT];
+    if (failed(a.st)) return;  // suffixes may be duplicated or stale
     int A = *a.A;
     int ntiles = (A + kWT - 1) / kWT;
     int nwarps = gridDim.x * kWarps;
@@ -1187,6 +1189,7 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
         a.p_grp = f.p_grp;
         a.write_rank = rank_mode;
         a.medium_max = S->tune.medium_max;
+        a.st = S->status;
         int grid = grid_for((A + kWT - 1) / kWT, kWarps, S->sms * 8);
         long long tiles_n = (A + kWT - 1) / kWT;
         // count: key and group rank of every slot; 12 bytes of partials per tile
@@ -1231,10 +1234,18 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
                   k_rank_fixup<<<grid_for(N, kThreads, S->sms * 16), kThreads, 0, st>>>((int)N, f.SA, f.R));
         fixed_up = true;
     };
+    DevStatus& hst = *reinterpret_cast<DevStatus*>(S->pin_rd + S->cap_blocks + 64);
     for (;;) {
         e = cudaMemcpyAsync(hcnt, S->counters, sizeof(int) * CNT_SLOTS, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&hst, S->status, sizeof(hst), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return map_cuda_error(e);
+        if (hst.error) {
+            // the counters of a round that failed are not to be trusted
+            prof_flush(S);
+            if (debug_on()) debug_log("device status %d at %d detail %lld", hst.error, hst.where, hst.detail);
+            return hst.error;
+        }
         int A = hcnt[act];
         // the last split wrote A survivors (8 B) and A_prev - A suffix-array
         // entries (4 B), and 4 B of rank per slot of round 0's split (none on
@@ -1286,7 +1297,6 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
               k_extract<<<grid_for(N, kThreads, S->sms * 16), kThreads, 0, st>>>(
                   (int)N, f.SA, f.R, d_T, S->blk_off, nb, d_U, S->blk_idx, aux_rate ? S->blk_aux_rate : nullptr,
                   S->blk_aux_off, S->aux, S->status));
-    DevStatus& hst = *reinterpret_cast<DevStatus*>(S->pin_rd + S->cap_blocks + 64);
     e = cudaMemcpyAsync(hcnt, S->blk_idx, sizeof(int) * nb, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&hst, S->status, sizeof(hst), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess && aux_out && aux_total)

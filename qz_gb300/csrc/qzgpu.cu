@@ -636,6 +636,9 @@ int qzgpu_storage_set_param(qzgpu_storage* storage, const char* name, long long 
     } else if (k == "ruler_stride_log2") {
         if (value < 3 || value > 12) return QZGPU_BAD_PARAMETER;
         each([&](Tune& t) { t.ruler_log2 = (int)value; });
+    } else if (k == "lookback_test") {
+        if (value < 0 || value > 1) return QZGPU_BAD_PARAMETER;
+        each([&](Tune& t) { t.lookback_test = (int)value; });
     } else {
         return QZGPU_BAD_PARAMETER;
     }
@@ -652,6 +655,7 @@ long long qzgpu_storage_get_param(const qzgpu_storage* storage, const char* name
     if (k == "tile_ctas_per_sm") return t.tile_ctas_per_sm;
     if (k == "medium_max") return t.medium_max;
     if (k == "ruler_stride_log2") return t.ruler_log2;
+    if (k == "lookback_test") return t.lookback_test;
     if (k == "lanes") return (long long)storage->lanes.size();
     return QZGPU_BAD_PARAMETER;
 }

@@ -363,8 +363,9 @@ __global__ void __launch_bounds__(kThreads, 3) k_big_pass0(BigArgs a, uint32_t* 
 
 // One stable 8-bit pass with decoupled look-back.
 __global__ void __launch_bounds__(kThreads, 4) k_big_pass(BigArgs a, const uint32_t* __restrict__ h4, int pass,
-                                                       unsigned epoch, BigBuffers bb, unsigned long long* status,
-                                                       unsigned* ticket, DevStatus* st) {
+                                                          unsigned epoch, BigBuffers bb, unsigned long long* status,
+                                                          unsigned* ticket, DevStatus* st, unsigned spin_limit,
+                                                          int silent_tile) {
     __shared__ uint32_t skey[kOT];
     __shared__ int sval[kOT];
     __shared__ uint32_t wcnt[kWarps][256];
@@ -376,6 +377,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_big_pass(BigArgs a, const uint3
     const unsigned lt_mask = (1u << ln) - 1u;
     const int shift = 8 * pass;
     const unsigned long long ep = (unsigned long long)epoch << 34;
+    // an earlier pass that failed leaves keys whose digits no longer match the
+    // group histograms, so the positions below would not stay in the group
+    if (failed(st)) return;
     int TT = *a.ntiles, nseg = *a.nseg;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -439,21 +443,22 @@ __global__ void __launch_bounds__(kThreads, 4) k_big_pass(BigArgs a, const uint3
             // before it in the same group
             volatile unsigned long long* my = status + (size_t)tau * 256 + dg;
             uint32_t excl = 0;
+            const bool silent = j == silent_tile;  // failure-detection test only
             if (j == 0) {
                 *my = ep | kFlagInc | run;
             } else {
-                *my = ep | kFlagAgg | run;
+                if (!silent) *my = ep | kFlagAgg | run;
                 int p = tau - 1;
                 for (;;) {
                     volatile unsigned long long* q = status + (size_t)p * 256 + dg;
                     unsigned long long v = *q;
                     unsigned spins = 0;
-                    while (((v >> 34) != epoch || (v & (3ull << 32)) == 0) && spins < kSpinLimit) {
+                    while (((v >> 34) != epoch || (v & (3ull << 32)) == 0) && spins < spin_limit) {
                         __nanosleep(32);
                         v = *q;
                         ++spins;
                     }
-                    if (spins >= kSpinLimit) {
+                    if (spins >= spin_limit) {
                         report(st, QZGPU_TIMEOUT, 20, tau);
                         break;
                     }
@@ -461,7 +466,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_big_pass(BigArgs a, const uint3
                     if (v & kFlagInc) break;
                     --p;
                 }
-                *my = ep | kFlagInc | (excl + run);
+                if (!silent) *my = ep | kFlagInc | (excl + run);
             }
             uint32_t tot;
             dig_off[dg] = block_excl_sum(run, sh, &tot);
@@ -549,8 +554,10 @@ void sort_big_groups(Storage* S, const int2* list, const int* d_count, int host_
         if (epoch == 0) epoch = ++S->radix_epoch & 0x3fffffffu;
         unsigned* ticket = reinterpret_cast<unsigned*>(cnt + CNT_TICKET);
         cudaMemsetAsync(ticket, 0, sizeof(unsigned), st);
+        const bool test = S->tune.lookback_test && pass == 1;
         QZ_LAUNCH(S, st, "k_big_pass", 16 * elems,
-                  k_big_pass<<<pgrid, kThreads, 0, st>>>(a, h4, pass, epoch, bb, f.status64, ticket, S->status));
+                  k_big_pass<<<pgrid, kThreads, 0, st>>>(a, h4, pass, epoch, bb, f.status64, ticket, S->status,
+                                                         test ? 4096u : kSpinLimit, test ? 1 : -1));
     }
 }
 

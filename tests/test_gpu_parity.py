@@ -152,6 +152,27 @@ def test_decode_wrong_index_does_not_hang(gpu):
         assert e.code == native.QZGPU_DATA_CORRUPT
 
 
+def test_lookback_wait_runs_out_without_fault(gpu, oracle):
+    # Failure detection: in the test mode one tile of every large group never
+    # publishes its look-back status, so the tiles behind it give up after a
+    # short bounded wait; the call returns QZGPU_TIMEOUT (no fault, no hang)
+    # and the same storage sorts correctly once the mode is off.
+    rng = np.random.default_rng(5)
+    blocks = [rng.integers(0, 256, 1 << 20).astype(np.uint8)]  # one 2^20-slot group at the start
+    with bwt.Storage(len(blocks[0]), 1) as st:
+        st.set_param("lookback_test", 1)
+        with pytest.raises(native.QzGpuError) as e:
+            st.encode_batch(blocks)
+        assert e.value.code == native.QZGPU_TIMEOUT
+        st.set_param("lookback_test", 0)
+        us, idx = st.encode_batch(blocks)
+        ous, oidx = oracle.bwt_encode_batch(blocks)
+        assert idx == list(oidx)
+        assert (us[0] == ous[0]).all()
+        with pytest.raises(native.QzGpuError):
+            st.set_param("lookback_test", 2)
+
+
 @pytest.mark.parametrize("params", [
     {"medium_max": 64, "big_ctas_per_sm": 2, "ruler_stride_log2": 3},
     {"medium_max": 128, "tile_ctas_per_sm": 1, "ruler_stride_log2": 7, "fwd_sub_bytes": 1 << 20,
