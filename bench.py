@@ -235,6 +235,9 @@ def run_gpu(args, rank: int, world: int):
         st.decode_device(sizes, idx, d_U.data_ptr(), d_R.data_ptr(), sptr)
         return idx, fl + st.stats()["kernel_launches"]
 
+    for kv in args.param:
+        k, v = kv.split("=", 1)
+        st.set_param(k, int(v))
     # ---- autotuner (before warm-up; not timed)
     tuned = None
     if not args.no_autotune:
@@ -339,6 +342,9 @@ def run_gpu(args, rank: int, world: int):
                 else:
                     os.environ["QZGPU_LANES"] = old
             for k, v in (tuned or {}).items():
+                st1.set_param(k, int(v))
+            for kv in args.param:
+                k, v = kv.split("=", 1)
                 st1.set_param(k, int(v))
             st1.encode_device(sizes, d_T.data_ptr(), d_U.data_ptr(), sptr)
             st1.profile(True, only=top["name"])
@@ -628,6 +634,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default knobs")
+    ap.add_argument("--param", action="append", default=[], metavar="NAME=VALUE",
+                    help="set a storage knob (qzgpu_storage_set_param) before timing; repeatable")
     ap.add_argument("--plain-blocks", action="store_true",
                     help="also time the plain path: one forward + inverse call per block")
     args = ap.parse_args()

@@ -143,7 +143,7 @@ int qzgpu_storage_round_counts(const qzgpu_storage *storage, long long *active, 
 
 /* Runtime tuning of a storage (set by the autotuner, qz_gb300/autotune.py):
  *   "fwd_sub_bytes", "inv_sub_bytes"  block bytes per sub-batch taken by a lane
- *   "big_ctas_per_sm"                 persistent CTAs per SM of a radix pass (1..4)
+ *   "big_ctas_per_sm"                 persistent CTAs per SM of a radix pass (1..3)
  *   "tile_ctas_per_sm"                CTAs per SM of the one-CTA group sort (1..3)
  *   "medium_max"                      longest group sorted by one warp (64..512)
  *   "ruler_stride_log2"               inverse: a ruler every 2^v rows (3..12)

@@ -21,7 +21,7 @@ import numpy as np
 SPACE = {
     "fwd_sub_bytes": [16 << 20, 32 << 20, 64 << 20],
     "inv_sub_bytes": [16 << 20, 32 << 20, 64 << 20],
-    "big_ctas_per_sm": [2, 3, 4],
+    "big_ctas_per_sm": [2, 3],
     "tile_ctas_per_sm": [1, 2, 3],
     "medium_max": [64, 128, 256, 512],
     "ruler_stride_log2": [4, 5, 6],

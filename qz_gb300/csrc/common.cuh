@@ -62,6 +62,16 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
+// 4-byte asynchronous copy global -> shared memory.  The copy is visible to
+// the issuing thread after cp_async_wait_all(); other threads need a barrier
+// after that wait as well.
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // Block-wide exclusive sum over kThreads threads. `sh` needs kWarps+1 slots.
 // Returns the exclusive prefix for this thread; *total receives the sum.
 template <typename T>

@@ -63,6 +63,7 @@ struct FwdBuffers {
     uint32_t* llen;    // large: length per group -> workspace base
     uint32_t* ltbase;
     uint32_t* lwbase;
+    uint32_t* tseg;    // large: group of each look-back tile
     uint32_t* p_surv;  // split: per 256-slot warp tile
     int* p_sub;
     int* p_grp;
@@ -82,7 +83,7 @@ struct InvBuffers {
 
 // Runtime tuning knobs of a lane (set through qzgpu_storage_set_param).
 struct Tune {
-    int big_ctas_per_sm = 4;   // persistent CTAs of a look-back radix pass
+    int big_ctas_per_sm = 3;   // persistent CTAs of a look-back radix pass (59 KB of shared memory each)
     int tile_ctas_per_sm = 3;  // CTAs of the one-CTA group sort
     int medium_max = kMedMax;  // longest group sorted by one warp (64..512)
     int ruler_log2 = 5;        // inverse: a ruler every 2^ruler_log2 rows (3..12)

@@ -197,6 +197,7 @@ size_t layout(Storage* S, char* base, const Caps& c) {
     f.llen = cv.take<uint32_t>(c.large + 1);
     f.ltbase = cv.take<uint32_t>(c.large + 1);
     f.lwbase = cv.take<uint32_t>(c.large + 1);
+    f.tseg = cv.take<uint32_t>(c.big_tiles);
     size_t wt = c.N / 256 + 2;
     f.p_surv = cv.take<uint32_t>(wt);
     f.p_sub = cv.take<int>(wt);
@@ -625,7 +626,7 @@ int qzgpu_storage_set_param(qzgpu_storage* storage, const char* name, long long 
         if (value < (1 << 20)) return QZGPU_BAD_PARAMETER;
         (k[0] == 'f' ? storage->fwd_sub_bytes : storage->inv_sub_bytes) = value;
     } else if (k == "big_ctas_per_sm") {
-        if (value < 1 || value > 4) return QZGPU_BAD_PARAMETER;  // all CTAs must stay resident
+        if (value < 1 || value > 3) return QZGPU_BAD_PARAMETER;  // all CTAs must stay resident
         each([&](Tune& t) { t.big_ctas_per_sm = (int)value; });
     } else if (k == "tile_ctas_per_sm") {
         if (value < 1 || value > 3) return QZGPU_BAD_PARAMETER;

@@ -209,7 +209,10 @@ __global__ void __launch_bounds__(kThreads) k_big_hist(BigArgs a, const uint32_t
     __shared__ int s_seg;
     int TT = *a.ntiles, nseg = *a.nseg;
     for (int tau = blockIdx.x; tau < TT; tau += gridDim.x) {
-        if (threadIdx.x == 0) s_seg = big_seg_of_tile(a.tbase, nseg, (uint32_t)tau);
+        if (threadIdx.x == 0) {
+            s_seg = big_seg_of_tile(a.tbase, nseg, (uint32_t)tau);
+            a.tseg[tau] = (uint32_t)s_seg;  // the passes read it in one load
+        }
 #pragma unroll
         for (int p = 0; p < 4; ++p) h[p][threadIdx.x] = 0;
         __syncthreads();
@@ -294,14 +297,15 @@ __device__ __forceinline__ BigRoute big_route(const BigBuffers& bb, const int2 d
 __global__ void __launch_bounds__(kThreads, 3) k_big_pass0(BigArgs a, uint32_t* __restrict__ h4, BigBuffers bb) {
     __shared__ uint32_t skey[kOT];
     __shared__ int sval[kOT];
+    __shared__ int vst[kOT];  // the tile's values in slot order (asynchronous copies)
     __shared__ uint32_t cnt[256];
     __shared__ uint32_t gb[256];
     __shared__ uint32_t sh[kWarps + 1];
     __shared__ int s_seg;
     const unsigned w = warp_id(), ln = lane_id();
-    const int TT = *a.ntiles, nseg = *a.nseg;
+    const int TT = *a.ntiles;
     for (int tau = blockIdx.x; tau < TT; tau += gridDim.x) {
-        if (threadIdx.x == 0) s_seg = big_seg_of_tile(a.tbase, nseg, (uint32_t)tau);
+        if (threadIdx.x == 0) s_seg = (int)a.tseg[tau];
         cnt[threadIdx.x] = 0;
         __syncthreads();
         const int s = s_seg;
@@ -321,10 +325,12 @@ __global__ void __launch_bounds__(kThreads, 3) k_big_pass0(BigArgs a, uint32_t* 
         const int src = j * kOT;
         const int n = min(kOT, d.y - j * kOT);
         uint32_t kr[kOItems], rk[kOItems];
+        // keys to registers and values to shared memory, all in flight at once
 #pragma unroll
         for (int it = 0; it < kOItems; ++it) {
             int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
             kr[it] = i < n ? __ldcs(sk + src + i) : 0u;
+            if (i < n) cp_async4(vst + i, sv + src + i);
         }
 #pragma unroll
         for (int it = 0; it < kOItems; ++it) {
@@ -340,6 +346,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_big_pass0(BigArgs a, uint32_t* 
             cnt[threadIdx.x] = off;
             gb[threadIdx.x] = base - off;
         }
+        cp_async_wait_all();  // each thread reads back only the values it copied
         __syncthreads();
 #pragma unroll
         for (int it = 0; it < kOItems; ++it) {
@@ -347,7 +354,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_big_pass0(BigArgs a, uint32_t* 
             if (i < n) {
                 uint32_t lp = cnt[kr[it] & 255u] + rk[it];
                 skey[lp] = kr[it];
-                sval[lp] = __ldcs(sv + src + i);
+                sval[lp] = vst[i];
             }
         }
         __syncthreads();
@@ -362,12 +369,13 @@ __global__ void __launch_bounds__(kThreads, 3) k_big_pass0(BigArgs a, uint32_t* 
 }
 
 // One stable 8-bit pass with decoupled look-back.
-__global__ void __launch_bounds__(kThreads, 4) k_big_pass(BigArgs a, const uint32_t* __restrict__ h4, int pass,
+__global__ void __launch_bounds__(kThreads, 3) k_big_pass(BigArgs a, const uint32_t* __restrict__ h4, int pass,
                                                           unsigned epoch, BigBuffers bb, unsigned long long* status,
                                                           unsigned* ticket, DevStatus* st, unsigned spin_limit,
                                                           int silent_tile) {
     __shared__ uint32_t skey[kOT];
     __shared__ int sval[kOT];
+    __shared__ int vst[kOT];  // the tile's values in slot order (asynchronous copies)
     __shared__ uint32_t wcnt[kWarps][256];
     __shared__ uint32_t dig_off[256];
     __shared__ uint32_t gbase[256];
@@ -380,11 +388,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_big_pass(BigArgs a, const uint3
     // an earlier pass that failed leaves keys whose digits no longer match the
     // group histograms, so the positions below would not stay in the group
     if (failed(st)) return;
-    int TT = *a.ntiles, nseg = *a.nseg;
+    const int TT = *a.ntiles;
     for (;;) {
         if (threadIdx.x == 0) {
             s_tau = (int)atomicAdd(ticket, 1u);
-            s_seg = s_tau < TT ? big_seg_of_tile(a.tbase, nseg, (uint32_t)s_tau) : 0;
+            s_seg = s_tau < TT ? (int)a.tseg[s_tau] : 0;
         }
 #pragma unroll
         for (int q = 0; q < kWarps; ++q) wcnt[q][threadIdx.x] = 0;
@@ -409,11 +417,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_big_pass(BigArgs a, const uint3
         int srcbase = j * kOT;
         int cnt = min(kOT, d.y - j * kOT);
         uint32_t rk[kOItems], kr[kOItems];
-        // all of the tile's keys in flight at once, then the ranking
+        // all of the tile's keys (to registers) and values (to shared memory)
+        // in flight at once, then the ranking
 #pragma unroll
         for (int it = 0; it < kOItems; ++it) {
             int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
             kr[it] = i < cnt ? __ldg(srck + srcbase + i) : 0u;
+            if (i < cnt) cp_async4(vst + i, srcv + srcbase + i);
         }
 #pragma unroll
         for (int it = 0; it < kOItems; ++it) {
@@ -472,6 +482,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_big_pass(BigArgs a, const uint3
             dig_off[dg] = block_excl_sum(run, sh, &tot);
             gbase[dg] = h4[((size_t)s * 4 + pass) * 256 + dg] + excl;
         }
+        cp_async_wait_all();  // each thread reads back only the values it copied
         __syncthreads();
 #pragma unroll
         for (int it = 0; it < kOItems; ++it) {
@@ -481,7 +492,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_big_pass(BigArgs a, const uint3
                 unsigned dg = (kv >> shift) & 255u;
                 uint32_t lp = dig_off[dg] + wcnt[w][dg] + rk[it];
                 skey[lp] = kv;
-                sval[lp] = __ldg(srcv + srcbase + i);
+                sval[lp] = vst[i];
             }
         }
         __syncthreads();
@@ -534,7 +545,7 @@ void sort_big_groups(Storage* S, const int2* list, const int* d_count, int host_
         scan_exclusive(S, f.ltc, f.ltbase, 0, d_count, (uint32_t*)(cnt + CNT_LTILES), st);
         scan_exclusive(S, f.llen, f.lwbase, 0, d_count, nullptr, st);
     }
-    BigArgs a{list, d_count, f.ltbase, f.lwbase, cnt + CNT_LTILES, f.gmask};
+    BigArgs a{list, d_count, f.ltbase, f.lwbase, cnt + CNT_LTILES, f.gmask, f.tseg};
     BigBuffers bb{key, val, {f.wsk[0], f.wsk[1]}, {f.wsv[0], f.wsv[1]}};
     uint32_t* h4 = f.h4;
     cudaMemsetAsync(h4, 0, sizeof(uint32_t) * 1024 * (size_t)host_count, st);
@@ -546,8 +557,8 @@ void sort_big_groups(Storage* S, const int2* list, const int* d_count, int host_
     // digit is constant in a group are skipped for that group)
     QZ_LAUNCH(S, st, "k_big_pass0", 16 * elems, k_big_pass0<<<grid, kThreads, 0, st>>>(a, h4, bb));
     // passes 1..3: stable, decoupled look-back; a persistent grid of resident
-    // CTAs (64 registers and 43 KB of shared memory per CTA fit four per SM),
-    // tiles taken by ticket
+    // CTAs (59 KB of shared memory per CTA: three fit an SM), tiles taken by
+    // ticket
     int pgrid = sms * S->tune.big_ctas_per_sm;
     for (int pass = 1; pass < 4; ++pass) {
         unsigned epoch = ++S->radix_epoch & 0x3fffffffu;

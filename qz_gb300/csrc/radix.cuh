@@ -11,6 +11,7 @@ struct BigArgs {
     const uint32_t* wbase;   // first workspace slot of each group
     const int* ntiles;       // total tiles (device)
     uint32_t* gmask;         // per group: passes whose digit is not constant (bit p)
+    uint32_t* tseg;          // group of each tile (written by the histogram kernel)
 };
 
 // Where a group's slots are before / after one of its needed passes: the first

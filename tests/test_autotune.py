@@ -7,7 +7,7 @@ from qz_gb300 import autotune
 
 class FakeStorage:
     def __init__(self):
-        self.p = {"fwd_sub_bytes": 64 << 20, "inv_sub_bytes": 64 << 20, "big_ctas_per_sm": 4,
+        self.p = {"fwd_sub_bytes": 64 << 20, "inv_sub_bytes": 64 << 20, "big_ctas_per_sm": 3,
                   "tile_ctas_per_sm": 3, "medium_max": 512, "ruler_stride_log2": 5}
 
     def set_param(self, k, v):
