@@ -448,8 +448,8 @@ __global__ void __launch_bounds__(kThreads) k_sort_straddle(const int* __restric
 // equal across the whole group are skipped.
 constexpr size_t kMedWarpSmem = (size_t)kMedMax * 8 + 256 * 4;
 
-__device__ __forceinline__ void warp_radix_sort(uint32_t* __restrict__ key, int* __restrict__ W, int s, int len,
-                                                unsigned char* wsm) {
+__device__ __forceinline__ void warp_radix_sort(const uint32_t* skey, const int* sW, uint32_t* key, int* W, int s,
+                                                int len, unsigned char* wsm) {
     unsigned long long* buf = reinterpret_cast<unsigned long long*>(wsm);
     uint32_t* cnt = reinterpret_cast<uint32_t*>(buf + kMedMax);
     const int ln = (int)lane_id();
@@ -464,8 +464,8 @@ __device__ __forceinline__ void warp_radix_sort(uint32_t* __restrict__ key, int*
         kr[it] = 0;
         vr[it] = 0;
         if (it < nit && i < len) {
-            kr[it] = key[s + i];
-            vr[it] = W[s + i];
+            kr[it] = skey[s + i];
+            vr[it] = sW[s + i];
             kor |= kr[it];
             kand &= kr[it];
         }
@@ -535,11 +535,12 @@ __device__ __forceinline__ void warp_radix_sort(uint32_t* __restrict__ key, int*
     }
 }
 
-// Groups of 17..64 slots, one warp per listed group: each slot ranks itself by
-// counting smaller keys (ties by slot) over shuffled keys; one slot per lane
-// up to 32 slots, two above.
+// Groups of up to 64 slots (the split lists 17..64 here), one warp per listed
+// group: each slot ranks itself by counting smaller keys (ties by slot) over
+// shuffled keys; one slot per lane up to 32 slots, two above.  The group is
+// read from (skey, sW) and written to (key, W), which may be the same arrays.
 __global__ void __launch_bounds__(kThreads) k_sort_rbc(const int2* __restrict__ list, const int* __restrict__ d_count,
-                                                       uint32_t* __restrict__ key, int* __restrict__ W) {
+                                                       const uint32_t* skey, const int* sW, uint32_t* key, int* W) {
     int cnt = *d_count;
     const int nwarps = gridDim.x * kWarps;
     const int ln = (int)lane_id();
@@ -547,8 +548,8 @@ __global__ void __launch_bounds__(kThreads) k_sort_rbc(const int2* __restrict__ 
         int2 d = list[i];
         const int s = d.x, len = d.y;
         bool v0 = ln < len;
-        uint32_t k0 = v0 ? key[s + ln] : 0xffffffffu;
-        int w0 = v0 ? W[s + ln] : 0;
+        uint32_t k0 = v0 ? skey[s + ln] : 0xffffffffu;
+        int w0 = v0 ? sW[s + ln] : 0;
         int r0 = 0;
         if (len <= 32) {
             for (int j = 0; j < len; ++j) {
@@ -562,8 +563,8 @@ __global__ void __launch_bounds__(kThreads) k_sort_rbc(const int2* __restrict__ 
             continue;
         }
         bool v1 = ln + 32 < len;
-        uint32_t k1 = v1 ? key[s + ln + 32] : 0xffffffffu;
-        int w1 = v1 ? W[s + ln + 32] : 0;
+        uint32_t k1 = v1 ? skey[s + ln + 32] : 0xffffffffu;
+        int w1 = v1 ? sW[s + ln + 32] : 0;
         int r1 = 0;
         for (int j = 0; j < len; ++j) {
             uint32_t kj = __shfl_sync(0xffffffffu, j < 32 ? k0 : k1, j & 31);
@@ -583,15 +584,15 @@ __global__ void __launch_bounds__(kThreads) k_sort_rbc(const int2* __restrict__ 
 
 // Groups of 65..512 slots, one warp per listed group: warp_radix_sort.
 __global__ void __launch_bounds__(kThreads, 3) k_sort_medium(const int2* __restrict__ list,
-                                                          const int* __restrict__ d_count,
-                                                          uint32_t* __restrict__ key, int* __restrict__ W) {
+                                                          const int* __restrict__ d_count, const uint32_t* skey,
+                                                          const int* sW, uint32_t* key, int* W) {
     extern __shared__ __align__(16) unsigned char msm[];
     int cnt = *d_count;
     const int nwarps = gridDim.x * kWarps;
     unsigned char* wsm = msm + warp_id() * kMedWarpSmem;
     for (int i = blockIdx.x * kWarps + (int)warp_id(); i < cnt; i += nwarps) {
         int2 d = list[i];
-        warp_radix_sort(key, W, d.x, d.y, wsm);
+        warp_radix_sort(skey, sW, key, W, d.x, d.y, wsm);
     }
 }
 
@@ -1007,6 +1008,31 @@ int grid_for(long long work, int per_cta, int cap) {
     return (int)g;
 }
 
+}  // namespace
+
+void sort_rbc_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
+                     const uint32_t* skey, const int* sval, uint32_t* key, int* val, cudaStream_t st) {
+    if (host_count <= 0) return;
+    QZ_LAUNCH(S, st, "k_sort_rbc", 16 * elems + 8ll * host_count,
+              k_sort_rbc<<<grid_for(host_count, kWarps, S->sms * 16), kThreads, 0, st>>>(list, d_count, skey, sval,
+                                                                                        key, val));
+}
+
+void sort_medium_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
+                        const uint32_t* skey, const int* sval, uint32_t* key, int* val, cudaStream_t st) {
+    if (host_count <= 0) return;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_sort_medium, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kWarps * kMedWarpSmem));
+        attr = true;
+    }
+    QZ_LAUNCH(S, st, "k_sort_medium", 16 * elems + 8ll * host_count,
+              k_sort_medium<<<grid_for(host_count, kWarps, S->sms * 16), kThreads, kWarps * kMedWarpSmem, st>>>(
+                  list, d_count, skey, sval, key, val));
+}
+
+namespace {
+
 // Sorts every group (key, W) in place in compact slot space.  hc: host copy
 // of the counters (list lengths, slots per class); A: active slots.
 void sort_groups(Storage* S, const int* hc, int A, const int* d_A, uint32_t* key, int* W, const int* G,
@@ -1014,30 +1040,16 @@ void sort_groups(Storage* S, const int* hc, int A, const int* d_A, uint32_t* key
     FwdBuffers& f = S->f;
     int* cnt = S->counters;
     const int sms = S->sms;
-    int nmd = hc[CNT_MED], nlg = hc[CNT_LARGE], nrb = hc[CNT_PAIR];
     long long small_el = (long long)A - hc[CNT_PAIR_ELEMS] - hc[CNT_MED_ELEMS] - hc[CNT_TILE_ELEMS] -
                          hc[CNT_LARGE_ELEMS];
-    if (nrb > 0)
-        QZ_LAUNCH(S, st, "k_sort_rbc", 16ll * hc[CNT_PAIR_ELEMS] + 8ll * nrb,
-                  k_sort_rbc<<<grid_for(nrb, kWarps, sms * 16), kThreads, 0, st>>>(f.list_rbc, cnt + CNT_PAIR, key,
-                                                                                  W));
+    sort_rbc_groups(S, f.list_rbc, cnt + CNT_PAIR, hc[CNT_PAIR], hc[CNT_PAIR_ELEMS], key, W, key, W, st);
     // every slot: group rank read; small groups: key and suffix read and written
     if (small_el > 0 && !small_done)
         QZ_LAUNCH(S, st, "k_sort_small", 4ll * A + 16ll * small_el,
                   k_sort_small<<<grid_for(A, kThreads, sms * 16), kThreads, 0, st>>>(d_A, G, key, W));
-    if (nmd > 0) {
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(k_sort_medium, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(kWarps * kMedWarpSmem));
-            attr = true;
-        }
-        QZ_LAUNCH(S, st, "k_sort_medium", 16ll * hc[CNT_MED_ELEMS] + 8ll * nmd,
-                  k_sort_medium<<<grid_for(nmd, kWarps, sms * 16), kThreads, kWarps * kMedWarpSmem, st>>>(
-                      f.list_med, cnt + CNT_MED, key, W));
-    }
-    sort_tile_groups(S, f.list_tile, cnt + CNT_TILE, hc[CNT_TILE], hc[CNT_TILE_ELEMS], key, W, st);
-    sort_big_groups(S, f.list_large, cnt + CNT_LARGE, nlg, hc[CNT_LARGE_ELEMS], key, W, st);
+    sort_medium_groups(S, f.list_med, cnt + CNT_MED, hc[CNT_MED], hc[CNT_MED_ELEMS], key, W, key, W, st);
+    sort_tile_groups(S, f.list_tile, cnt + CNT_TILE, hc[CNT_TILE], hc[CNT_TILE_ELEMS], key, W, key, W, st);
+    sort_big_groups(S, f.list_large, cnt + CNT_LARGE, hc[CNT_LARGE], hc[CNT_LARGE_ELEMS], key, W, st);
 }
 
 }  // namespace

@@ -36,9 +36,12 @@ constexpr unsigned kSpinLimit = 1u << 24;
 // One CTA per group of kTileMin..kOT slots: stable 8-bit passes in shared
 // memory (warp match-based ranks; ping-pong key/value buffers).  Each warp
 // takes an equal contiguous share of the group (a multiple of 32 slots), and
-// digits that are equal across the whole group are skipped.
+// digits that are equal across the whole group are skipped.  The group is
+// read from (skey, sval) and written to (key, val) at the same slots; the two
+// may be the same arrays.
 __global__ void __launch_bounds__(kThreads) k_tile_sort(const int2* __restrict__ list, const int* __restrict__ d_count,
-                                                        uint32_t* __restrict__ key, int* __restrict__ val) {
+                                                        const uint32_t* skey, const int* sval, uint32_t* key,
+                                                        int* val) {
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t* k0 = reinterpret_cast<uint32_t*>(smem);
     int* v0 = reinterpret_cast<int*>(k0 + kOT);
@@ -56,9 +59,9 @@ __global__ void __launch_bounds__(kThreads) k_tile_sort(const int2* __restrict__
         int s = d.x, len = d.y;
         uint32_t kor = 0, kand = 0xffffffffu;
         for (int i = threadIdx.x; i < len; i += kThreads) {
-            uint32_t k = key[s + i];
+            uint32_t k = skey[s + i];
             k0[i] = k;
-            v0[i] = val[s + i];
+            v0[i] = sval[s + i];
             kor |= k;
             kand &= k;
         }
@@ -168,28 +171,51 @@ __global__ void __launch_bounds__(kThreads) k_big_prep(const int2* __restrict__ 
 // tile counts and lengths), the total tile count, and cleared pass masks.
 constexpr int kPlanMaxGroups = 32768;
 
-__global__ void __launch_bounds__(kThreads) k_big_plan(const int2* __restrict__ list, const int* __restrict__ d_count,
-                                                       uint32_t* __restrict__ tbase, uint32_t* __restrict__ wbase,
-                                                       uint32_t* __restrict__ gmask, int* __restrict__ total_tiles) {
-    __shared__ uint32_t sh[kWarps + 1];
+constexpr int kPlanThreads = 1024;
+
+__global__ void __launch_bounds__(kPlanThreads) k_big_plan(const int2* __restrict__ list,
+                                                           const int* __restrict__ d_count,
+                                                           uint32_t* __restrict__ tbase, uint32_t* __restrict__ wbase,
+                                                           uint32_t* __restrict__ gmask,
+                                                           int* __restrict__ total_tiles) {
+    __shared__ uint32_t sht[kPlanThreads / 32 + 1], shw[kPlanThreads / 32 + 1];
     const int cnt = *d_count;
-    uint32_t ct = 0, cw = 0;
-    for (int b0 = 0; b0 < cnt; b0 += kThreads) {
-        const int i = b0 + threadIdx.x;
-        const uint32_t len = i < cnt ? (uint32_t)list[i].y : 0u;
-        const uint32_t tl = (len + kOT - 1) / kOT;
-        uint32_t tt, tw;
-        const uint32_t et = block_excl_sum(tl, sh, &tt);
-        const uint32_t ew = block_excl_sum(len, sh, &tw);
-        if (i < cnt) {
-            tbase[i] = ct + et;
-            wbase[i] = cw + ew;
-            gmask[i] = 0;
-        }
-        ct += tt;
-        cw += tw;
+    // each thread owns a contiguous run of groups: its loads are issued
+    // together, then one scan over the block
+    const int per = (cnt + kPlanThreads - 1) / kPlanThreads;
+    const int i0 = min(cnt, (int)threadIdx.x * per), i1 = min(cnt, i0 + per);
+    uint32_t st = 0, sw = 0;
+#pragma unroll 8
+    for (int i = i0; i < i1; ++i) {
+        const uint32_t len = (uint32_t)__ldg(&list[i].y);
+        st += (len + kOT - 1) / kOT;
+        sw += len;
     }
-    if (threadIdx.x == 0) *total_tiles = (int)ct;
+    const unsigned ln = lane_id(), wp = warp_id();
+    const uint32_t it = warp_incl_sum(st), iw = warp_incl_sum(sw);
+    if (ln == 31) {
+        sht[wp] = it;
+        shw[wp] = iw;
+    }
+    __syncthreads();
+    if (wp == 0) {
+        const uint32_t t = sht[ln], w = shw[ln];
+        const uint32_t ti = warp_incl_sum(t), wi = warp_incl_sum(w);
+        sht[ln] = ti - t;
+        shw[ln] = wi - w;
+        if (ln == 31) *total_tiles = (int)ti;
+    }
+    __syncthreads();
+    uint32_t et = sht[wp] + it - st, ew = shw[wp] + iw - sw;
+#pragma unroll 8
+    for (int i = i0; i < i1; ++i) {
+        const uint32_t len = (uint32_t)__ldg(&list[i].y);
+        tbase[i] = et;
+        wbase[i] = ew;
+        gmask[i] = 0;
+        et += (len + kOT - 1) / kOT;
+        ew += len;
+    }
 }
 
 // largest s in [0, n) with tbase[s] <= tau
@@ -521,13 +547,38 @@ int grid_cap(long long work, int per_cta, int cap) {
 size_t tile_sort_smem() { return (size_t)kOT * 16 + sizeof(uint32_t) * kWarps * 256; }
 
 void sort_tile_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
-                      uint32_t* key, int* val, cudaStream_t st) {
+                      const uint32_t* skey, const int* sval, uint32_t* key, int* val, cudaStream_t st) {
     if (host_count <= 0) return;
-    cudaFuncSetAttribute(k_tile_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_sort_smem());
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_tile_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_sort_smem());
+        attr = true;
+    }
     QZ_LAUNCH(S, st, "k_tile_sort", 16 * elems,
-              k_tile_sort<<<grid_cap(host_count, 1, S->sms * S->tune.tile_ctas_per_sm), kThreads, tile_sort_smem(), st>>>(list, d_count,
-                                                                                                  key, val));
+              k_tile_sort<<<grid_cap(host_count, 1, S->sms * S->tune.tile_ctas_per_sm), kThreads, tile_sort_smem(),
+                            st>>>(list, d_count, skey, sval, key, val));
 }
+
+namespace {
+
+// Tile bases (and the total tile count) per listed group, cleared digit masks.
+void big_plan(Storage* S, const int2* list, const int* d_count, int host_count, cudaStream_t st) {
+    FwdBuffers& f = S->f;
+    int* cnt = S->counters;
+    if (host_count <= kPlanMaxGroups) {
+        QZ_LAUNCH(S, st, "k_big_plan", 20ll * host_count,
+                  k_big_plan<<<1, kPlanThreads, 0, st>>>(list, d_count, f.ltbase, f.lwbase, f.gmask,
+                                                         cnt + CNT_LTILES));
+    } else {
+        QZ_LAUNCH(S, st, "k_big_prep", 20ll * host_count,
+                  k_big_prep<<<grid_cap(host_count, kThreads, S->sms * 4), kThreads, 0, st>>>(list, d_count, f.ltc,
+                                                                                             f.llen, f.gmask));
+        scan_exclusive(S, f.ltc, f.ltbase, 0, d_count, (uint32_t*)(cnt + CNT_LTILES), st);
+        scan_exclusive(S, f.llen, f.lwbase, 0, d_count, nullptr, st);
+    }
+}
+
+}  // namespace
 
 void sort_big_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
                      uint32_t* key, int* val, cudaStream_t st) {
@@ -535,16 +586,7 @@ void sort_big_groups(Storage* S, const int2* list, const int* d_count, int host_
     FwdBuffers& f = S->f;
     int* cnt = S->counters;
     const int sms = S->sms;
-    if (host_count <= kPlanMaxGroups) {
-        QZ_LAUNCH(S, st, "k_big_plan", 20ll * host_count,
-                  k_big_plan<<<1, kThreads, 0, st>>>(list, d_count, f.ltbase, f.lwbase, f.gmask, cnt + CNT_LTILES));
-    } else {
-        QZ_LAUNCH(S, st, "k_big_prep", 20ll * host_count,
-                  k_big_prep<<<grid_cap(host_count, kThreads, sms * 4), kThreads, 0, st>>>(list, d_count, f.ltc,
-                                                                                          f.llen, f.gmask));
-        scan_exclusive(S, f.ltc, f.ltbase, 0, d_count, (uint32_t*)(cnt + CNT_LTILES), st);
-        scan_exclusive(S, f.llen, f.lwbase, 0, d_count, nullptr, st);
-    }
+    big_plan(S, list, d_count, host_count, st);
     BigArgs a{list, d_count, f.ltbase, f.lwbase, cnt + CNT_LTILES, f.gmask, f.tseg};
     BigBuffers bb{key, val, {f.wsk[0], f.wsk[1]}, {f.wsv[0], f.wsv[1]}};
     uint32_t* h4 = f.h4;

@@ -24,10 +24,21 @@ struct BigBuffers {
     int* wsv[2];
 };
 
-// Groups of kMedMax+1 .. kOT slots (one CTA each, all passes in shared memory).
+// Listed groups sorted by key: read from (skey, sval) and written to (key,
+// val) at the same slots (the two may be the same arrays).  host_count and
+// elems are host copies (or bounds) of the group and slot counts; d_count is
+// the device count the kernels read.
+// Groups of medium_max+1 .. kOT slots (one CTA each, all passes in shared memory).
 void sort_tile_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
-                      uint32_t* key, int* val, cudaStream_t st);
-// Groups longer than kOT slots (one decoupled look-back pass per digit).
+                      const uint32_t* skey, const int* sval, uint32_t* key, int* val, cudaStream_t st);
+// Groups of 17..64 slots (one warp each, rank by count; fwd.cu).
+void sort_rbc_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
+                     const uint32_t* skey, const int* sval, uint32_t* key, int* val, cudaStream_t st);
+// Groups of 65..medium_max slots (one warp each, LSD radix in shared memory; fwd.cu).
+void sort_medium_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
+                        const uint32_t* skey, const int* sval, uint32_t* key, int* val, cudaStream_t st);
+// Groups longer than kOT slots, in place in (key, val) (one decoupled
+// look-back pass per digit).
 void sort_big_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
                      uint32_t* key, int* val, cudaStream_t st);
 size_t tile_sort_smem();

@@ -175,6 +175,7 @@ def test_lookback_wait_runs_out_without_fault(gpu, oracle):
 
 @pytest.mark.parametrize("params", [
     {"medium_max": 64, "big_ctas_per_sm": 2, "ruler_stride_log2": 3},
+    {"medium_max": 512, "big_ctas_per_sm": 3, "fwd_sub_bytes": 1 << 20},
     {"medium_max": 128, "tile_ctas_per_sm": 1, "ruler_stride_log2": 7, "fwd_sub_bytes": 1 << 20,
      "inv_sub_bytes": 1 << 20},
     {"medium_max": 256, "big_ctas_per_sm": 1, "ruler_stride_log2": 4},
