@@ -182,6 +182,28 @@ def run_reference(args, rank: int):
     print(json.dumps(line), flush=True)
 
 
+# --------------------------------------------------------------------------- replicas
+
+
+def max_over_ranks(values, dist=None):
+    """Per-rank timings reduced element-wise to the slowest rank's (gloo
+    all-reduce MAX): the job takes as long as its slowest replica."""
+    vals = [float(v) for v in values]
+    if dist is None:
+        return vals
+    import torch
+
+    t = torch.tensor(vals, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def job_rate(world: int, nbytes: int, steps: int, seconds: float) -> float:
+    """Whole-job MB/s: each of `world` replicas processes the same `nbytes`
+    per step (weak scaling), timed by the slowest rank."""
+    return world * nbytes * steps / seconds / 1e6
+
+
 # --------------------------------------------------------------------------- GPU path
 
 
@@ -302,11 +324,8 @@ def run_gpu(args, rank: int, world: int):
     inv_ms = sum(ev[3 * k + 1].elapsed_time(ev[3 * k + 2]) for k in range(args.steps))
     prof_top = st.profile_read(reset=True)
     st.profile(False)
-    if dist:
-        t = torch.tensor([total_ms, fwd_ms, inv_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, fwd_ms, inv_ms = t.tolist()
-    value = world * N * args.steps / (total_ms / 1e3) / 1e6
+    total_ms, fwd_ms, inv_ms = max_over_ranks([total_ms, fwd_ms, inv_ms], dist)
+    value = job_rate(world, N, args.steps, total_ms / 1e3)
 
     # ---- roofline of the dominant kernel (event-timed inside the timed region)
     peak, peak_kind = load_peak()
@@ -416,11 +435,8 @@ def run_gpu(args, rank: int, world: int):
         if not all(np.array_equal(a, b) for a, b in zip(back, blocks)):
             raise SystemExit("host round trip mismatch")
         e2e_s = t1 - t0
-        if dist:
-            t = torch.tensor([e2e_s], dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        e2e = {"value": round(world * N * args.steps / e2e_s / 1e6, 3), "unit": "MB/s",
+        e2e_s = max_over_ranks([e2e_s], dist)[0]
+        e2e = {"value": round(job_rate(world, N, args.steps, e2e_s), 3), "unit": "MB/s",
                "h2d_bytes_per_step": 2 * N, "d2h_bytes_per_step": 2 * N,
                "api": "qzgpu_bwt_encode_batch + qzgpu_bwt_decode_batch (pinned host buffers, reused)"}
 
@@ -446,8 +462,8 @@ def run_gpu(args, rank: int, world: int):
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "tuned": tuned if tuned else st.params(),
                        "step": "forward BWT of all blocks + inverse BWT of the result"},
-            "fwd_mb_s": round(world * N * args.steps / (fwd_ms / 1e3) / 1e6, 3),
-            "inv_mb_s": round(world * N * args.steps / (inv_ms / 1e3) / 1e6, 3),
+            "fwd_mb_s": round(job_rate(world, N, args.steps, fwd_ms / 1e3), 3),
+            "inv_mb_s": round(job_rate(world, N, args.steps, inv_ms / 1e3), 3),
             "rounds": fwd_stats["rounds"] if fwd_stats else None,
             "active_per_round": rounds_active,
             "gpu_launches": launches,
