@@ -1,6 +1,8 @@
 """One rank of the replica timing test, launched by torch.distributed.run with
 the gloo backend (no GPU): each rank reports made-up per-rank timings, reduces
-them with bench.max_over_ranks and prints the result as one JSON line."""
+them with bench.max_over_ranks and writes the result as JSON to
+<out_dir>/rank<r>.json (one file per rank: printed lines of two ranks can
+interleave)."""
 import json
 import os
 import sys
@@ -20,7 +22,8 @@ def main():
     mine = [100.0 * (rank + 1), 50.0 - rank]
     out = bench.max_over_ranks(mine, dist)
     rate = bench.job_rate(world, 1_000_000, 4, out[0] / 1e3)
-    print(json.dumps({"rank": rank, "world": world, "mine": mine, "max": out, "rate": rate}), flush=True)
+    with open(os.path.join(sys.argv[1], f"rank{rank}.json"), "w") as f:
+        json.dump({"rank": rank, "world": world, "mine": mine, "max": out, "rate": rate}, f)
     dist.barrier()
     dist.destroy_process_group()
 

@@ -39,10 +39,14 @@ def test_job_rate_counts_every_replica():
     assert bench.max_over_ranks([3, 1.5]) == [3.0, 1.5]  # one process: unchanged
 
 
-def test_max_over_ranks_two_gloo_ranks():
-    r = _torchrun([os.path.join("tests", "replica_worker.py")])
+def test_max_over_ranks_two_gloo_ranks(tmp_path):
+    r = _torchrun([os.path.join("tests", "replica_worker.py"), str(tmp_path)])
     assert r.returncode == 0, r.stderr[-2000:]
-    lines = {d["rank"]: d for d in _json_lines(r.stdout)}
+    lines = {}
+    for k in range(2):
+        with open(tmp_path / f"rank{k}.json") as f:
+            d = json.load(f)
+        lines[d["rank"]] = d
     assert sorted(lines) == [0, 1]
     for d in lines.values():
         assert d["world"] == 2
