@@ -5,9 +5,10 @@
 // QZGPU_LANES overrides).  Each
 // lane is a full scratch set (Storage) with its own stream and a persistent
 // worker thread.  A batch is cut into sub-batches of at most lane_bytes block
-// bytes (blocks kept whole); lanes take sub-batches as they become free, so
-// the latency-bound phases of one sub-batch (dependent gathers, per-round host
-// reads of the counters) overlap with the work of the others on the device.
+// bytes (blocks kept whole); lanes take sub-batches, largest first, as they
+// become free, so the latency-bound phases of one sub-batch (dependent
+// gathers, per-round host reads of the counters) overlap with the work of the
+// others on the device.
 // Lane 0 is sized for the whole capacity and alone takes a block larger than
 // lane_bytes.
 #include <algorithm>
@@ -105,6 +106,7 @@ int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned cha
     struct Sub {
         int b0, b1;
         long long off, bytes;
+        int seq;  // place in the order the lanes take sub-batches
     };
     std::vector<Sub> big, small;
     long long off = 0;
@@ -113,31 +115,50 @@ int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned cha
         int b1 = b0;
         long long bytes = 0;
         while (b1 < nb && (b1 == b0 || bytes + n[b1] <= limit)) bytes += n[b1++];
-        (bytes > E->lane_bytes ? big : small).push_back(Sub{b0, b1, off, bytes});
+        (bytes > E->lane_bytes ? big : small).push_back(Sub{b0, b1, off, bytes, 0});
         off += bytes;
         b0 = b1;
+    }
+    // Lanes take the largest sub-batches first (longest-processing-time order,
+    // bytes standing for time), so that no large sub-batch starts last and
+    // runs alone while the other lanes idle.  Every block keeps its place in
+    // the input and output buffers; only the order of work changes.
+    std::stable_sort(small.begin(), small.end(), [](const Sub& x, const Sub& y) { return x.bytes > y.bytes; });
+    // lane 0 takes the sub-batches above lane_bytes before any other
+    std::vector<const Sub*> order;
+    for (Sub& sb : big) {
+        sb.seq = (int)order.size();
+        order.push_back(&sb);
+    }
+    for (Sub& sb : small) {
+        sb.seq = (int)order.size();
+        order.push_back(&sb);
     }
     // Output pages of host buffers that nothing has touched yet (fresh
     // allocations) make device-to-host copies fault page by page, several
     // times slower than into resident pages.  A host thread touches one byte
-    // per page of every output buffer, in block order, while the device
-    // works; a lane waits for its blocks before it copies them out.
-    std::atomic<int> touched{nb};
+    // per page of every output buffer, sub-batch by sub-batch in the order the
+    // lanes take them, while the device works; a lane waits for its
+    // sub-batch's pages before it copies the blocks out.
+    const int nsub = (int)order.size();
+    std::atomic<int> touched{nsub};  // sub-batches (in `order`) whose pages are touched
     std::mutex tmu;
     std::condition_variable tcv;
     std::thread toucher;
     if (host && off >= kTouchMinBytes) {
         touched = 0;
         toucher = std::thread([&] {
-            for (int b = 0; b < nb; ++b) {
-                // in place (output = input): the caller's pages are resident
-                // and still hold the input
-                volatile unsigned char* p = hout[b];
-                if (hout[b] != hin[b])
-                    for (long long o = 0; o < n[b]; o += 4096) p[o] = 0;
+            for (int k = 0; k < nsub; ++k) {
+                for (int b = order[k]->b0; b < order[k]->b1; ++b) {
+                    // in place (output = input): the caller's pages are
+                    // resident and still hold the input
+                    volatile unsigned char* p = hout[b];
+                    if (hout[b] != hin[b])
+                        for (long long o = 0; o < n[b]; o += 4096) p[o] = 0;
+                }
                 {
                     std::lock_guard<std::mutex> lk(tmu);
-                    touched.store(b + 1);
+                    touched.store(k + 1);
                 }
                 tcv.notify_all();
             }
@@ -159,7 +180,7 @@ int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned cha
         if (host) {
             const std::function<void()> wait_out = [&] {
                 std::unique_lock<std::mutex> lk(tmu);
-                tcv.wait(lk, [&] { return touched.load() >= sb.b1; });
+                tcv.wait(lk, [&] { return touched.load() > sb.seq; });
             };
             rc = forward ? encode_host(S, cnt, hin + sb.b0, hout + sb.b0, n + sb.b0, idx + sb.b0, nullptr, nullptr,
                                        &wait_out)

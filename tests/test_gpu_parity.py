@@ -298,6 +298,28 @@ def test_block_above_lane_size(gpu, oracle):
         assert all((x == y).all() for x, y in zip(back, blocks))
 
 
+def test_lanes_take_largest_sub_batches_first(gpu, oracle):
+    # a three-lane storage (capacity above 64 MiB) with 1 MiB sub-batches:
+    # twelve uneven blocks (11 MB of fresh host output, so the output pages are
+    # touched on a host thread in the order the lanes work) are cut into
+    # sub-batches that the lanes take largest first; every block must come
+    # back in its own place
+    rng = np.random.default_rng(7)
+    sizes = [int(x) for x in rng.integers(1000, 1_800_000, 12)]
+    g = synth.uniform_genome(300_000, seed=8)
+    blocks = [synth.sample_reads(g, s // 150 + 1, seed=9 + i)[:s] for i, s in enumerate(sizes)]
+    with bwt.Storage(65 << 20, 16) as st:
+        assert st.get_param("lanes") == 3
+        st.set_param("fwd_sub_bytes", 1 << 20)
+        st.set_param("inv_sub_bytes", 1 << 20)
+        us, idx = st.encode_batch(blocks)
+        ous, oidx = oracle.bwt_encode_batch(blocks)
+        assert idx == list(oidx)
+        assert all((u == ou).all() for u, ou in zip(us, ous))
+        back = st.decode_batch(us, idx)
+        assert all((x == y).all() for x, y in zip(back, blocks))
+
+
 def test_ultra_block_round_trip(gpu):
     # a 300 MiB block (qz's reorder levels use blocks up to 750 MiB): the
     # inverse of the forward is the input (size-independent property; the
