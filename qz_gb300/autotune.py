@@ -67,10 +67,14 @@ def apply(storage, params: dict) -> None:
             storage.set_param(k, int(v))
 
 
-def tune(storage, run, key: str | None = None, reps: int = 2, use_cache: bool = True, log=None) -> dict:
+def tune(storage, run, key: str | None = None, reps: int = 3, use_cache: bool = True, log=None,
+         min_gain: float = 0.02) -> dict:
     """Coordinate descent over SPACE.  `run()` performs one forward + inverse of
-    the workload on `storage` and returns its duration in ms.  Returns the best
-    parameters (already applied to the storage) and records them under `key`."""
+    the workload on `storage` and returns its duration in ms; each candidate
+    keeps the best of `reps` runs, and replaces the current setting only if it
+    is faster by more than `min_gain` (a step of the multi-lane engine varies
+    by a few percent from run to run).  Returns the best parameters (already
+    applied to the storage) and records them under `key`."""
     cache = load_cache() if use_cache else {}
     if key and use_cache and key in cache:
         best = cache[key]["params"]
@@ -94,7 +98,7 @@ def tune(storage, run, key: str | None = None, reps: int = 2, use_cache: bool = 
             trials += 1
             if log:
                 log(f"autotune {k}={v}: {ms:.2f} ms (best {best_ms:.2f})")
-            if ms < best_ms * 0.99:
+            if ms < best_ms * (1.0 - min_gain):
                 best_ms, current = ms, cand
     apply(storage, current)
     if key:
