@@ -62,6 +62,7 @@ struct Server {
 
 void Server::worker(int i) {
     Storage* S = slots[i].get();
+    cudaSetDevice(S->device);  // a new thread starts on device 0
     std::vector<long long> take;
     std::vector<const unsigned char*> ins;
     std::vector<unsigned char*> outs;
