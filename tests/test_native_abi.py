@@ -71,3 +71,41 @@ def test_no_cpu_fallback_without_gpu(lib):
     with pytest.raises(native.QzGpuError) as e:
         bwt.bwt_encode(b"ACGTACGT")
     assert e.value.code in (native.QZGPU_GPU_NOT_SUPPORTED, native.QZGPU_GPU_ERROR)
+
+
+C_CALLER = r"""
+/* A plain C caller of the boundary: the header is valid C and every entry
+ * point links from a C program (the binding a Rust, Go or C host would make). */
+#include <stdio.h>
+#include "qzgpu.h"
+
+int main(int argc, char **argv) {
+    if (argc < 2) return 0; /* linked, not run: no GPU needed */
+    unsigned char t[8] = "ACGTACGT";
+    unsigned char num = 0;
+    int idx[4];
+    int rc = qzgpu_bwt_encode(t, 8, &num, idx, QZGPU_FEATURE_FASTMODE);
+    qzgpu_storage *st = 0;
+    qzgpu_storage_create(&st, 1 << 20, 4);
+    qzgpu_storage_destroy(st);
+    qzgpu_streams_info info;
+    qzgpu_fastq_streams(t, 0, 0, 0, 0, 0, 0, 0, &info);
+    printf("%d %s\n", rc, qzgpu_error_string(rc));
+    return qzgpu_bwt_decode_noalloc(0, 0, 0, 1, 0);
+}
+"""
+
+
+def test_c_program_compiles_and_links(lib, tmp_path):
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(native.LIB_PATH)
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-pedantic", "-I", os.path.join(ROOT, "include"),
+                        str(src), "-o", str(exe), "-L", libdir, "-lqzgpu", f"-Wl,-rpath,{libdir}"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    # the program loads the library (no compute call without an argument)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+
