@@ -14,7 +14,9 @@
  *
  *   - suffix sorting by induced sorting (SA-IS, Nong, Zhang & Chan 2009), with
  *     an implicit end sentinel smaller than every byte;
- *   - a brute-force suffix sort (direct comparison) as an independent check;
+ *   - a brute-force suffix sort (direct comparison) as an independent check,
+ *     and prefix doubling (Manber & Myers 1993) as a second one for sizes
+ *     brute force cannot reach;
  *   - the libsais BWT output convention (libsais is libbsc's CPU sorter,
  *     build.rs:62): U[0] = T[n-1], then the last column of the sorted matrix
  *     with the sentinel row dropped, and the primary index = 1 + the rank of
@@ -202,6 +204,60 @@ int oracle_suffix_array_bruteforce(const uint8_t *T, int32_t *SA, int32_t n)
     g_bf_text = T;
     g_bf_n = n;
     qsort(SA, (size_t)n, sizeof(int32_t), bf_cmp);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Prefix doubling (Manber & Myers 1993), a second independent sorter for    */
+/* sizes brute force cannot reach.                                           */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * Round h sorts the suffixes by their first 2h symbols: the pair (rank of
+ * suffix i, rank of suffix i+h), where a suffix that ends inside the first h
+ * symbols gets the smallest second key (the end sentinel).  Each round is two
+ * stable counting sorts (second key, then first key) and a dense re-ranking;
+ * it stops once every rank is distinct.  O(n log n) time, 4n ints of memory.
+ */
+int oracle_suffix_array_doubling(const uint8_t *T, int32_t *SA, int32_t n)
+{
+    if (n < 0 || (n > 0 && (!T || !SA))) return ORACLE_BAD_PARAMETER;
+    if (n == 0) return 0;
+    size_t cn = (size_t)(n > 256 ? n : 256) + 2;
+    int32_t *rk = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+    int32_t *nrk = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+    int32_t *tmp = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+    int32_t *cnt = (int32_t *)malloc(cn * sizeof(int32_t));
+    if (!rk || !nrk || !tmp || !cnt) {
+        free(rk); free(nrk); free(tmp); free(cnt);
+        return ORACLE_NOT_ENOUGH_MEMORY;
+    }
+    for (int32_t i = 0; i < n; ++i) rk[i] = T[i];
+    int32_t K = 256; /* ranks are in [0, K) */
+    for (int64_t h = 1;; h <<= 1) {
+        /* second key: 0 when suffix i ends within h symbols, else 1 + rank */
+#define KEY2(i) ((int64_t)(i) + h < n ? rk[(i) + h] + 1 : 0)
+        memset(cnt, 0, ((size_t)K + 1) * sizeof(int32_t));
+        for (int32_t i = 0; i < n; ++i) cnt[KEY2(i)]++;
+        for (int32_t c = 0, run = 0; c <= K; ++c) { int32_t t = cnt[c]; cnt[c] = run; run += t; }
+        for (int32_t i = 0; i < n; ++i) tmp[cnt[KEY2(i)]++] = i;
+        memset(cnt, 0, (size_t)K * sizeof(int32_t));
+        for (int32_t i = 0; i < n; ++i) cnt[rk[i]]++;
+        for (int32_t c = 0, run = 0; c < K; ++c) { int32_t t = cnt[c]; cnt[c] = run; run += t; }
+        for (int32_t j = 0; j < n; ++j) { int32_t i = tmp[j]; SA[cnt[rk[i]]++] = i; }
+        int32_t r = 0;
+        nrk[SA[0]] = 0;
+        for (int32_t j = 1; j < n; ++j) {
+            int32_t a = SA[j - 1], b = SA[j];
+            if (rk[a] != rk[b] || KEY2(a) != KEY2(b)) ++r;
+            nrk[b] = r;
+        }
+#undef KEY2
+        memcpy(rk, nrk, (size_t)n * sizeof(int32_t));
+        K = r + 1;
+        if (K == n || h >= n) break;
+    }
+    free(rk); free(nrk); free(tmp); free(cnt);
     return 0;
 }
 

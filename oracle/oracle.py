@@ -43,13 +43,15 @@ def lib():
             i32p = ctypes.POINTER(ctypes.c_int32)
             L.oracle_suffix_array.argtypes = [u8p, i32p, ctypes.c_int32]
             L.oracle_suffix_array_bruteforce.argtypes = [u8p, i32p, ctypes.c_int32]
+            L.oracle_suffix_array_doubling.argtypes = [u8p, i32p, ctypes.c_int32]
             L.oracle_bwt_encode.argtypes = [u8p, u8p, ctypes.c_int32, ctypes.c_int32, i32p]
             L.oracle_bwt_decode.argtypes = [u8p, u8p, ctypes.c_int32, ctypes.c_int32]
             L.oracle_bwt_batch.argtypes = [
                 ctypes.c_int, ctypes.c_int32, ctypes.POINTER(u8p), ctypes.POINTER(u8p), i32p, i32p, i32p,
                 ctypes.c_int32,
             ]
-            for f in (L.oracle_suffix_array, L.oracle_suffix_array_bruteforce, L.oracle_bwt_encode,
+            for f in (L.oracle_suffix_array, L.oracle_suffix_array_bruteforce, L.oracle_suffix_array_doubling,
+                      L.oracle_bwt_encode,
                       L.oracle_bwt_decode, L.oracle_bwt_batch):
                 f.restype = ctypes.c_int
             _lib = L
@@ -70,10 +72,16 @@ def as_u8(data) -> np.ndarray:
     return np.ascontiguousarray(data, dtype=np.uint8)
 
 
-def suffix_array(data, brute: bool = False) -> np.ndarray:
+def suffix_array(data, brute: bool = False, method: str = "sais") -> np.ndarray:
+    """Suffix array with an implicit smallest end sentinel.  method: "sais"
+    (induced sorting), "doubling" (prefix doubling) or "brute" (direct
+    comparison, small inputs); brute=True is the same as method="brute"."""
     t = as_u8(data)
     sa = np.empty(max(len(t), 1), dtype=np.int32)
-    f = lib().oracle_suffix_array_bruteforce if brute else lib().oracle_suffix_array
+    if brute:
+        method = "brute"
+    f = {"sais": lib().oracle_suffix_array, "doubling": lib().oracle_suffix_array_doubling,
+         "brute": lib().oracle_suffix_array_bruteforce}[method]
     rc = f(_u8(t), _i32(sa), len(t))
     if rc:
         raise RuntimeError(f"oracle suffix array failed: {rc}")

@@ -1,6 +1,7 @@
 """The CPU oracle, pinned before it is trusted: golden vectors (definition-level
 BWT, the reference's BSC test strings), brute-force suffix order, exhaustive
-small alphabets, and the inverse."""
+small alphabets, a second independent suffix sorter (prefix doubling) at
+megabyte sizes, and the inverse."""
 import itertools
 import json
 import os
@@ -77,3 +78,38 @@ def test_batch_matches_single(oracle):
             assert (u == uu).all() and i == ii
     back = oracle.bwt_decode_batch(us, idx, threads=4)
     assert all((x == y).all() for x, y in zip(back, blocks))
+
+
+def test_doubling_agrees_with_bruteforce(oracle):
+    rng = np.random.default_rng(31)
+    for n in (1, 2, 3, 17, 100, 1000):
+        for alpha in (1, 2, 4, 256):
+            t = rng.integers(0, alpha, n).astype(np.uint8)
+            assert (oracle.suffix_array(t, method="doubling") == oracle.suffix_array(t, brute=True)).all()
+
+
+@pytest.mark.parametrize("kind", ["dna", "quality", "header", "repeat", "period3", "single", "random"])
+def test_sais_agrees_with_doubling_at_megabytes(oracle, kind):
+    # two independent suffix sorters agree at sizes brute force cannot reach
+    from qz_gb300 import synth
+
+    n = 1_500_000
+    if kind == "dna":
+        t = synth.sample_reads(synth.uniform_genome(200_000, seed=41), n // 150, seed=42)
+    elif kind == "quality":
+        t = synth.quality_stream(n // 132, seed=43)
+    elif kind == "header":
+        t = synth.header_stream(n // 45, seed=44)
+    elif kind == "repeat":
+        t = synth.sample_reads(synth.repeat_genome(100_000, seed=45), n // 250, seed=46, read_len=250)
+    elif kind == "period3":
+        t = np.resize(np.frombuffer(b"ACG", np.uint8), n)
+    elif kind == "single":
+        t = np.full(n, ord("N"), np.uint8)
+    else:
+        t = np.random.default_rng(47).integers(0, 256, n).astype(np.uint8)
+    sa = oracle.suffix_array(t)
+    assert (sa == oracle.suffix_array(t, method="doubling")).all()
+    u, idx = oracle.bwt_encode(t)
+    assert (oracle.bwt_decode(u, idx) == t).all()
+
