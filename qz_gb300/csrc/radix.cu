@@ -13,12 +13,17 @@
 //     are stable: each tile takes a ticket in order, publishes its digit
 //     counts, and looks back over the tiles before it in the same group for
 //     its exclusive prefix (decoupled look-back), then scatters through shared
-//     memory so that each digit's run leaves as coalesced writes.
+//     memory so that each digit's run leaves as coalesced writes.  A tile
+//     loads its keys to registers and its values to shared memory (4-byte
+//     cp.async) together, and finds its group through the tile table the
+//     histogram kernel writes.
 //
 // Look-back waits are bounded: a tile only waits on tiles that took earlier
 // tickets, which publish their counts before they wait themselves; a wait that
 // exceeds its iteration limit records QZGPU_TIMEOUT in the status word and the
-// tile returns.
+// tile goes on (its positions stay inside its group), and the kernels whose
+// stores such a failure could misplace return at entry once the status word
+// is set; the host reads it after every round.
 #include "engine.h"
 #include "radix.cuh"
 #include "scan.cuh"
