@@ -16,6 +16,7 @@
 #include <cstdlib>
 
 #include "engine.h"
+#include "plan.h"
 
 namespace qz {
 
@@ -102,38 +103,18 @@ int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned cha
         cudaError_t e = cudaStreamSynchronize(user_stream);
         if (e != cudaSuccess) return map_cuda_error(e);
     }
-    // sub-batches: consecutive whole blocks, at most lane_bytes (a larger block alone)
-    struct Sub {
-        int b0, b1;
-        long long off, bytes;
-        int seq;  // place in the order the lanes take sub-batches
-    };
+    // sub-batches: consecutive whole blocks, at most lane_bytes (a larger block
+    // alone); lane 0 takes those above lane_bytes first, the lanes then take
+    // the others largest first
+    using Sub = SubBatch;
     std::vector<Sub> big, small;
-    long long off = 0;
-    long long limit = std::min(E->lane_bytes, forward ? E->fwd_sub_bytes : E->inv_sub_bytes);
-    for (int b0 = 0; b0 < nb;) {
-        int b1 = b0;
-        long long bytes = 0;
-        while (b1 < nb && (b1 == b0 || bytes + n[b1] <= limit)) bytes += n[b1++];
-        (bytes > E->lane_bytes ? big : small).push_back(Sub{b0, b1, off, bytes, 0});
-        off += bytes;
-        b0 = b1;
-    }
-    // Lanes take the largest sub-batches first (longest-processing-time order,
-    // bytes standing for time), so that no large sub-batch starts last and
-    // runs alone while the other lanes idle.  Every block keeps its place in
-    // the input and output buffers; only the order of work changes.
-    std::stable_sort(small.begin(), small.end(), [](const Sub& x, const Sub& y) { return x.bytes > y.bytes; });
-    // lane 0 takes the sub-batches above lane_bytes before any other
+    plan_sub_batches(nb, n, std::min(E->lane_bytes, forward ? E->fwd_sub_bytes : E->inv_sub_bytes), E->lane_bytes,
+                     &big, &small);
     std::vector<const Sub*> order;
-    for (Sub& sb : big) {
-        sb.seq = (int)order.size();
-        order.push_back(&sb);
-    }
-    for (Sub& sb : small) {
-        sb.seq = (int)order.size();
-        order.push_back(&sb);
-    }
+    for (const Sub& sb : big) order.push_back(&sb);
+    for (const Sub& sb : small) order.push_back(&sb);
+    long long off = 0;
+    for (int b = 0; b < nb; ++b) off += n[b];
     // Output pages of host buffers that nothing has touched yet (fresh
     // allocations) make device-to-host copies fault page by page, several
     // times slower than into resident pages.  A host thread touches one byte
