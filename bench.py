@@ -4,11 +4,23 @@ One step = forward BWT of every block of the workload followed by the inverse
 BWT of the result, device-resident inputs (the round trip is checked on the
 device after warm-up).  Default workload: one qz chunk of 2.5M synthetic
 150 bp reads split into qz's sequence / quality / header streams and cut into
-25 MiB blocks (about 33 blocks, 818 MB), all blocks in one batched call.
+25 MiB blocks (33 blocks, 818 MB), all blocks in one batched call.
+
+Beside the timed step the default line carries:
+  * parity: the GPU's output of the blocks the CPU baseline sorted, compared
+    with the oracle's (the run fails on a mismatch);
+  * roofline of the dominant kernel (event-timed inside the timed region, and
+    alone on a one-lane storage) and a clean per-kernel table from that
+    one-lane pass;
+  * e2e through the host-buffer C ABI (copies inside the timed region);
+  * batched_vs_plain: the 256-block uneven batch (1 KB-25 MiB), autotuned
+    batched calls against one call per block on the same inputs;
+  * serving: saturation MB/s and p50/p99 latency at 0.5x / 1.0x / 1.5x load.
 
 Prints one JSON line (rank 0).  `--impl reference` times the CPU path instead
-(the C oracle over all host threads, one block per thread as qz runs libbsc
-under rayon), on a bounded sample of the same workload.
+(the C oracle built with -O3 and host-core tuning, one block per host thread as
+qz runs libbsc under rayon), each step on a bounded, kind-stratified sample of
+the same workload that rotates through all its blocks.
 """
 from __future__ import annotations
 
@@ -55,6 +67,14 @@ def make_workload(name: str, reads: int):
     else:
         raise SystemExit(f"unknown config {name}")
     return [b for _, b in blocks], [k for k, _ in blocks], desc
+
+
+def workload_config(desc: str, blocks, world: int) -> dict:
+    """The `config` object both arms print for the same workload."""
+    return {"workload": desc, "blocks": len(blocks), "bytes": int(sum(len(b) for b in blocks)),
+            "l2": "inputs larger than L2 (workload bytes and scratch exceed 126 MB)",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "step": "forward BWT of all blocks + inverse BWT of the result"}
 
 
 # --------------------------------------------------------------------------- clocks
@@ -115,32 +135,53 @@ class ClockSampler:
 # --------------------------------------------------------------------------- CPU path
 
 
-def cpu_sample(blocks, kinds, cores: int):
-    """Bounded sample: one block per host thread, kinds interleaved like the workload."""
-    order = sorted(range(len(blocks)), key=lambda i: (i % 3, i))
+def stratified_order(kinds) -> list[int]:
+    """Block order that interleaves the kinds in the workload's proportions
+    (block i of a kind with c blocks sits at (i + 0.5) / c), so that any run of
+    consecutive entries has about the workload's kind mix."""
+    seen, pos = {}, []
+    count = {k: kinds.count(k) for k in set(kinds)}
+    for i, k in enumerate(kinds):
+        j = seen.get(k, 0)
+        seen[k] = j + 1
+        pos.append(((j + 0.5) / count[k], i))
+    return [i for _, i in sorted(pos)]
+
+
+def cpu_sample(blocks, kinds, cores: int, step: int = 0):
+    """Step `step`'s bounded sample: `cores` blocks (one per host thread),
+    consecutive in the stratified order and rotating with the step, so that
+    successive steps cover every block of the workload."""
+    order = stratified_order(kinds)
     take = max(1, min(len(blocks), cores))
-    idx = sorted(order[:take])
-    return [blocks[i] for i in idx], [kinds[i] for i in idx]
+    idx = sorted(order[(step * take + j) % len(order)] for j in range(take))
+    return idx, [blocks[i] for i in idx], [kinds[i] for i in idx]
 
 
 def time_cpu(sample, cores: int):
+    """Oracle forward + inverse of the sample over `cores` host threads (the
+    host-tuned build).  Returns (forward s, inverse s, U list, indexes)."""
     from oracle import oracle as O
 
     O.build()
     t0 = time.perf_counter()
-    us, idx = O.bwt_encode_batch(sample, threads=cores)
+    us, idx = O.bwt_encode_batch(sample, threads=cores, tuned=True)
     t1 = time.perf_counter()
-    back = O.bwt_decode_batch(us, idx, threads=cores)
+    back = O.bwt_decode_batch(us, idx, threads=cores, tuned=True)
     t2 = time.perf_counter()
     for a, b in zip(back, sample):
         if not np.array_equal(a, b):
             raise SystemExit("CPU round trip mismatch")
-    return t1 - t0, t2 - t1
+    return t1 - t0, t2 - t1, us, [int(i) for i in idx]
 
 
 def cpu_desc(sample, kinds) -> str:
     mb = sum(len(b) for b in sample) / 1e6
-    return f"{len(sample)} blocks ({mb:.1f} MB; " + ", ".join(f"{k}" for k in kinds) + ")"
+    mix = {k: kinds.count(k) for k in sorted(set(kinds))}
+    return f"{len(sample)} blocks ({mb:.1f} MB; " + ", ".join(f"{v} {k}" for k, v in mix.items()) + ")"
+
+
+CPU_BUILD = "C oracle (SA-IS + LF inverse), gcc -O3 tuned for the host core; oracle CPU, not libbsc"
 
 
 def cpu_model() -> str:
@@ -154,29 +195,39 @@ def cpu_model() -> str:
     return "unknown"
 
 
-def run_reference(args, rank: int):
+def run_reference(args, rank: int, world: int):
     if rank != 0:
         return
     blocks, kinds, desc = make_workload(args.config, args.reads)
     cores = os.cpu_count() or 1
-    sample, skinds = cpu_sample(blocks, kinds, cores)
-    nbytes = sum(len(b) for b in sample)
-    for _ in range(args.warmup):
+    for w in range(args.warmup):
+        _, sample, _ = cpu_sample(blocks, kinds, cores, step=w)
         time_cpu(sample, cores)
-    times = []
-    for _ in range(args.steps):
-        te, ti = time_cpu(sample, cores)
+    times, nbytes, covered = [], 0, set()
+    mix = []
+    for k in range(args.steps):
+        ids, sample, skinds = cpu_sample(blocks, kinds, cores, step=args.warmup + k)
+        te, ti, _, _ = time_cpu(sample, cores)
         times.append(te + ti)
+        nbytes += sum(len(b) for b in sample)
+        covered.update(ids)
+        mix += skinds
     total = sum(times)
-    value = nbytes * args.steps / total / 1e6
+    value = nbytes / total / 1e6
+    per_step = nbytes / args.steps
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "MB/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": desc, "sample_blocks": len(sample), "sample_bytes": nbytes},
+        "config": workload_config(desc, blocks, world),
         "cpu_baseline": {"value": round(value, 3), "unit": "MB/s", "cores": cores, "kind": "port",
-                         "sample": cpu_desc(sample, skinds) + "; oracle CPU, not libbsc (libbsc is not in the "
-                                                             "reference tree)", "cpu": cpu_model()},
+                         "sample": (f"each step {min(cores, len(blocks))} of the {len(blocks)} blocks "
+                                    f"({per_step / 1e6:.1f} MB), one per host thread, consecutive in a "
+                                    f"kind-stratified order that rotates with the step; {len(covered)} of "
+                                    f"{len(blocks)} blocks covered, timed mix "
+                                    + ", ".join(f"{mix.count(k)} {k}" for k in sorted(set(mix)))
+                                    + f"; forward + inverse; {CPU_BUILD} (libbsc is not in the reference tree)"),
+                         "cpu": cpu_model()},
         "e2e": {"value": round(value, 3), "unit": "MB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -217,7 +268,8 @@ def load_peak():
 
 
 def load_traffic():
-    """Per-launch DRAM bytes of kernels from a committed ncu summary, if any."""
+    """Per-launch DRAM bytes of kernels from a committed ncu summary, if any:
+    {kernel: {"dram_bytes_per_launch", "alg_bytes_per_launch", ...}}."""
     p = os.path.join(ROOT, "profiles", "dram_traffic.json")
     try:
         with open(p) as f:
@@ -226,276 +278,108 @@ def load_traffic():
         return {}
 
 
-def run_gpu(args, rank: int, world: int):
+def one_lane_storage(bwt, nbytes, nblocks, tuned, params):
+    old = os.environ.get("QZGPU_LANES")
+    os.environ["QZGPU_LANES"] = "1"
+    try:
+        st1 = bwt.Storage(nbytes, nblocks)
+    finally:
+        if old is None:
+            del os.environ["QZGPU_LANES"]
+        else:
+            os.environ["QZGPU_LANES"] = old
+    for k, v in (tuned or {}).items():
+        st1.set_param(k, int(v))
+    for kv in params:
+        k, v = kv.split("=", 1)
+        st1.set_param(k, int(v))
+    return st1
+
+
+def autotune_storage(st, step, blocks, dev, stream, reps=3):
+    import torch
+
+    from qz_gb300 import autotune
+
+    def run_once():
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1)
+
+    run_once()
+    key = autotune.signature(blocks, torch.cuda.get_device_name(dev))
+    return autotune.tune(st, run_once, key=key, use_cache=False, reps=reps)
+
+
+def batched_vs_plain(args, dev, stream):
+    """The uneven batch (256 blocks, 1 KB-25 MiB, DNA / quality / header):
+    autotuned batched calls against one forward + inverse call per block, on
+    the same device-resident inputs."""
     import torch
 
     from qz_gb300 import bwt
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("gloo")
-    blocks, kinds, desc = make_workload(args.config, args.reads)
+    blocks, _, desc = make_workload("uneven", args.reads)
     sizes = [len(b) for b in blocks]
     N = sum(sizes)
-    host = np.concatenate(blocks)
-    dev = torch.device("cuda", local)
-    d_T = torch.from_numpy(host).to(dev)
+    d_T = torch.from_numpy(np.concatenate(blocks)).to(dev)
     d_U = torch.empty_like(d_T)
     d_R = torch.empty_like(d_T)
-    bwt.init()
-    st = bwt.Storage(N, len(blocks))
-    stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
-
-    def step():
-        idx = st.encode_device(sizes, d_T.data_ptr(), d_U.data_ptr(), sptr)
-        fl = st.stats()["kernel_launches"]
-        st.decode_device(sizes, idx, d_U.data_ptr(), d_R.data_ptr(), sptr)
-        return idx, fl + st.stats()["kernel_launches"]
-
-    for kv in args.param:
-        k, v = kv.split("=", 1)
-        st.set_param(k, int(v))
-    # ---- autotuner (before warm-up; not timed)
-    tuned = None
-    if not args.no_autotune:
-        from qz_gb300 import autotune
-
-        def run_once():
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            step()
-            e1.record(stream)
-            torch.cuda.synchronize(dev)
-            return e0.elapsed_time(e1)
-
-        run_once()
-        key = autotune.signature(blocks, torch.cuda.get_device_name(dev))
-        tuned = autotune.tune(st, run_once, key=key, use_cache=False)
-    for _ in range(args.warmup):
-        idx, _ = step()
-    torch.cuda.synchronize(dev)
-    if not torch.equal(d_R, d_T):
-        raise SystemExit("GPU round trip mismatch")
-    fwd_stats = None
-
-    # ---- one profiled step (every launch bracketed by events): kernel table and
-    # the dominant kernel; not part of the timed region
-    st.profile(True)
-    st.profile_read(reset=True)
-    step()
-    torch.cuda.synchronize(dev)
-    prof_all = st.profile_read(reset=True)
-    dominant = prof_all[0]["name"] if prof_all else None
-
-    # ---- timed region (device-resident inputs, 818 MB > 126 MB L2); only the
-    # dominant kernel's launches carry events, for the roofline
-    clocks = ClockSampler(local)
-    st.profile(True, only=dominant)
-    st.profile_read(reset=True)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize(dev)
-    clocks.start()
-    time.sleep(0.3)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3 * args.steps + 1)]
-    launches = 0
-    ev[0].record(stream)
-    for k in range(args.steps):
-        idx = st.encode_device(sizes, d_T.data_ptr(), d_U.data_ptr(), sptr)
-        fwd_stats = st.stats()
-        rounds_active = st.round_counts()
-        launches += fwd_stats["kernel_launches"]
-        ev[3 * k + 1].record(stream)
-        st.decode_device(sizes, idx, d_U.data_ptr(), d_R.data_ptr(), sptr)
-        launches += st.stats()["kernel_launches"]
-        ev[3 * k + 2].record(stream)
-        ev[3 * k + 3].record(stream)
-    torch.cuda.synchronize(dev)
-    clk = clocks.stop()
-    if dist:
-        dist.barrier()
-    total_ms = ev[0].elapsed_time(ev[3 * args.steps])
-    fwd_ms = sum((ev[3 * k].elapsed_time(ev[3 * k + 1]) if k else ev[0].elapsed_time(ev[1])) for k in range(args.steps))
-    inv_ms = sum(ev[3 * k + 1].elapsed_time(ev[3 * k + 2]) for k in range(args.steps))
-    prof_top = st.profile_read(reset=True)
-    st.profile(False)
-    total_ms, fwd_ms, inv_ms = max_over_ranks([total_ms, fwd_ms, inv_ms], dist)
-    value = job_rate(world, N, args.steps, total_ms / 1e3)
-
-    # ---- roofline of the dominant kernel (event-timed inside the timed region)
-    peak, peak_kind = load_peak()
-    traffic = load_traffic()
-    kernels = []
-    for p in prof_all:
-        gbs = (p["alg_bytes"] / (p["ms"] / 1e3) / 1e9) if p["ms"] > 0 and p["alg_bytes"] > 0 else None
-        kernels.append({"name": p["name"], "launches": p["launches"], "ms": round(p["ms"], 3),
-                        "share": round(p["ms"] / max(sum(q["ms"] for q in prof_all), 1e-9), 4),
-                        "alg_gb_s": round(gbs, 1) if gbs else None})
-    top = prof_top[0] if prof_top else None
-    roof = None
-    if top:
-        per_launch_bytes = top["alg_bytes"] / max(top["launches"], 1)
-        avg_s = top["ms"] / max(top["launches"], 1) / 1e3
-        achieved = per_launch_bytes / avg_s / 1e9 if avg_s > 0 else 0.0
-        tr = traffic.get(top["name"])
-        roof = {"bound": "hbm", "kernel": top["name"], "achieved": round(achieved, 1), "peak": peak,
-                "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "alg_bytes_per_launch": int(per_launch_bytes), "launches_timed": top["launches"],
-                "traffic": (tr.get("bytes_per_launch") if isinstance(tr, dict) else tr)}
-        # the same kernel timed with the GPU to itself (a one-lane storage, one
-        # forward pass of the workload): its own rate, without the other lanes'
-        # kernels inside its event windows
-        if world == 1:
-            old = os.environ.get("QZGPU_LANES")
-            os.environ["QZGPU_LANES"] = "1"
-            try:
-                st1 = bwt.Storage(N, len(blocks))
-            finally:
-                if old is None:
-                    del os.environ["QZGPU_LANES"]
-                else:
-                    os.environ["QZGPU_LANES"] = old
-            for k, v in (tuned or {}).items():
-                st1.set_param(k, int(v))
-            for kv in args.param:
-                k, v = kv.split("=", 1)
-                st1.set_param(k, int(v))
-            st1.encode_device(sizes, d_T.data_ptr(), d_U.data_ptr(), sptr)
-            st1.profile(True, only=top["name"])
-            st1.profile_read(reset=True)
-            st1.encode_device(sizes, d_T.data_ptr(), d_U.data_ptr(), sptr)
-            torch.cuda.synchronize(dev)
-            p1 = st1.profile_read(reset=True)
-            st1.profile(False)
-            st1.close()
-            if p1 and p1[0]["launches"]:
-                b1 = p1[0]["alg_bytes"] / p1[0]["launches"]
-                s1 = p1[0]["ms"] / p1[0]["launches"] / 1e3
-                a1 = b1 / s1 / 1e9 if s1 > 0 else 0.0
-                roof["alone"] = {"achieved": round(a1, 1), "frac": round(a1 / peak, 4),
-                                 "launches": p1[0]["launches"],
-                                 "how": "one forward pass of the workload on a one-lane storage"}
-
-    # ---- plain one-block-per-call path on the same device-resident inputs
-    plain = None
-    if args.plain_blocks:
-        offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    with bwt.Storage(N, len(blocks)) as st:
+        def step():
+            idx = st.encode_device(sizes, d_T.data_ptr(), d_U.data_ptr(), sptr)
+            st.decode_device(sizes, idx, d_U.data_ptr(), d_R.data_ptr(), sptr)
 
         def plain_step():
             for b, n in enumerate(sizes):
-                if n == 0:
-                    continue
                 o = int(offs[b])
                 ix = st.encode_device([n], d_T.data_ptr() + o, d_U.data_ptr() + o, sptr)
                 st.decode_device([n], ix, d_U.data_ptr() + o, d_R.data_ptr() + o, sptr)
 
-        plain_step()
-        torch.cuda.synchronize(dev)
-        if not torch.equal(d_R, d_T):
-            raise SystemExit("plain-path round trip mismatch")
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
-            plain_step()
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-        pms = e0.elapsed_time(e1)
-        plain = {"value": round(N * args.steps / (pms / 1e3) / 1e6, 3), "unit": "MB/s",
-                 "ms_per_step": round(pms / args.steps, 3),
-                 "path": "one qzgpu_bwt_encode_device + qzgpu_bwt_decode_device call per block"}
+        tuned = None if args.no_autotune else autotune_storage(st, step, blocks, dev, stream, reps=2)
 
-    # ---- end to end through the host-buffer C ABI (copies inside the timed region)
-    e2e = None
-    if not args.no_e2e:
-        # pinned host buffers, allocated once and reused by every step: the
-        # step's inputs are copied to the device and its outputs back inside
-        # the library calls
-        def pinned(n):
-            return torch.empty(max(n, 1), dtype=torch.uint8, pin_memory=True).numpy()[:n]
+        def timed(fn, steps):
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize(dev)
+            d_R.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            if not torch.equal(d_R, d_T):
+                raise SystemExit("uneven batch round trip mismatch")
+            return e0.elapsed_time(e1) / steps
 
-        h_in = [pinned(len(b)) for b in blocks]
-        for h, b in zip(h_in, blocks):
-            h[:] = b
-        h_u = [pinned(len(b)) for b in blocks]
-        h_back = [pinned(len(b)) for b in blocks]
-        us, ix = st.encode_batch(h_in, out=h_u)
-        st.decode_batch(h_u, ix, out=h_back)
-        if dist:
-            dist.barrier()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            us, ix = st.encode_batch(h_in, out=h_u)
-            back = st.decode_batch(h_u, ix, out=h_back)
-        t1 = time.perf_counter()
-        if not all(np.array_equal(a, b) for a, b in zip(back, blocks)):
-            raise SystemExit("host round trip mismatch")
-        e2e_s = t1 - t0
-        e2e_s = max_over_ranks([e2e_s], dist)[0]
-        e2e = {"value": round(job_rate(world, N, args.steps, e2e_s), 3), "unit": "MB/s",
-               "h2d_bytes_per_step": 2 * N, "d2h_bytes_per_step": 2 * N,
-               "api": "qzgpu_bwt_encode_batch + qzgpu_bwt_decode_batch (pinned host buffers, reused)"}
-
-    # ---- CPU baseline on a bounded sample (rank 0, N=1 only)
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cores = os.cpu_count() or 1
-        sample, skinds = cpu_sample(blocks, kinds, cores)
-        te, ti = time_cpu(sample, cores)
-        cpu = {"value": round(sum(len(b) for b in sample) / (te + ti) / 1e6, 3), "unit": "MB/s", "cores": cores,
-               "kind": "port", "sample": cpu_desc(sample, skinds) + "; forward+inverse, oracle CPU, not libbsc",
-               "fwd_mb_s": round(sum(len(b) for b in sample) / te / 1e6, 3),
-               "inv_mb_s": round(sum(len(b) for b in sample) / ti / 1e6, 3), "cpu": cpu_model()}
-
-    if rank == 0:
-        line = {
-            "metric": METRIC, "value": round(value, 3), "unit": "MB/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u8",
-            "data": "synthetic (seeded reads of the workload's shape; no public dataset)",
-            "config": {"workload": desc, "blocks": len(blocks), "bytes": N,
-                       "l2": "inputs larger than L2 (workload bytes and scratch exceed 126 MB)",
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "tuned": tuned if tuned else st.params(),
-                       "step": "forward BWT of all blocks + inverse BWT of the result"},
-            "fwd_mb_s": round(job_rate(world, N, args.steps, fwd_ms / 1e3), 3),
-            "inv_mb_s": round(job_rate(world, N, args.steps, inv_ms / 1e3), 3),
-            "rounds": fwd_stats["rounds"] if fwd_stats else None,
-            "active_per_round": rounds_active,
-            "gpu_launches": launches,
-            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
-            "kernels": kernels[:12], "kernels_note": "one extra profiled step (events around every launch)",
-            "plain_per_block": plain,
-        }
-        print(json.dumps(line), flush=True)
-    st.close()
-    if dist:
-        dist.destroy_process_group()
+        bms = timed(step, max(args.steps // 2, 3))
+        pms = timed(plain_step, 2)
+    return {"workload": desc, "blocks": len(blocks), "bytes": N,
+            "batched_mb_s": round(N / bms / 1e3, 3), "batched_ms_per_step": round(bms, 3),
+            "plain_mb_s": round(N / pms / 1e3, 3), "plain_ms_per_step": round(pms, 3),
+            "batched_over_plain": round(pms / bms, 3), "tuned": tuned,
+            "plain_path": "one qzgpu_bwt_encode_device + qzgpu_bwt_decode_device call per block",
+            "step": "forward + inverse of every block, device-resident"}
 
 
-# --------------------------------------------------------------------------- serving
-
-
-def run_serve(args, rank: int, world: int):
+def serve_sweep(nreq: int, loads, warmup: int, slots: int):
     """Poisson arrivals of block requests (70% forward, 30% inverse of blocks
     produced beforehand), sizes log-uniform 64 KiB-25 MiB, mixed DNA / quality /
-    header content; served by qzgpu_server_* with continuous batching."""
-    import torch
-
+    header content, served by qzgpu_server_* with continuous batching.  Returns
+    the saturation point (all requests at once) and one point per offered
+    load (a fraction of the saturation rate)."""
     from qz_gb300 import bwt, synth
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    bwt.init()
-    reqs = synth.serving_requests(args.requests, rate_per_s=1.0, seed=6)
-    # inverse requests carry previously produced BWTs (made before timing)
+    reqs = synth.serving_requests(nreq, rate_per_s=1.0, seed=6)
     inv_in = {}
     inv_ids = [i for i, r in enumerate(reqs) if r[1] == "inv"]
-    with bwt.Storage(256 << 20, 256) as st:
+    with bwt.Storage(256 << 20, 256) as st:  # the inverse requests' inputs, made before timing
         chunk, used = [], 0
         for i in inv_ids + [None]:
             if i is None or used + len(reqs[i][3]) > (256 << 20):
@@ -509,7 +393,7 @@ def run_serve(args, rank: int, world: int):
                 used += len(reqs[i][3])
     total_bytes = sum(len(r[3]) for r in reqs)
     mean_bytes = total_bytes / len(reqs)
-    srv = bwt.Server(hbm_budget=0, max_slots=args.slots, slot_bytes=64 << 20, slot_blocks=256)
+    srv = bwt.Server(hbm_budget=0, max_slots=slots, slot_bytes=64 << 20, slot_blocks=256)
 
     def submit(i):
         _, op, _, block = reqs[i]
@@ -519,7 +403,6 @@ def run_serve(args, rank: int, world: int):
         return srv.submit_forward(block)
 
     def run_point(gaps):
-        # gaps: seconds between arrivals (None = all at once)
         tickets = [None] * len(reqs)
         lat = []
         done = threading.Event()
@@ -550,33 +433,277 @@ def run_serve(args, rank: int, world: int):
                 "p50_ms": round(lat[len(lat) // 2], 3), "p99_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),
                 "wall_s": round(t1 - t0, 3)}
 
-    for _ in range(max(1, args.warmup)):
-        run_point(None)
-    sat = run_point(None)
-    sat_rate = sat["mb_s"] * 1e6 / mean_bytes  # requests per second at saturation
-    rng = np.random.default_rng(60)
-    unit_gaps = rng.exponential(1.0, len(reqs))
-    points = []
-    for frac in (0.25, 0.5, 0.75, 1.0, 1.25, 1.5):
-        gaps = unit_gaps / (frac * sat_rate)
-        pt = run_point(gaps)
-        pt["offered_load"] = frac
-        pt["offered_mb_s"] = round(frac * sat["mb_s"], 3)
-        points.append(pt)
-    stats = srv.stats()
-    srv.close()
+    try:
+        for _ in range(max(1, warmup)):
+            run_point(None)
+        sat = run_point(None)
+        sat_rate = sat["mb_s"] * 1e6 / mean_bytes  # requests per second at saturation
+        rng = np.random.default_rng(60)
+        unit_gaps = rng.exponential(1.0, len(reqs))
+        points = []
+        for frac in loads:
+            pt = run_point(unit_gaps / (frac * sat_rate))
+            pt["offered_load"] = frac
+            pt["offered_mb_s"] = round(frac * sat["mb_s"], 3)
+            points.append(pt)
+        stats = srv.stats()
+    finally:
+        srv.close()
+    return {"requests": len(reqs), "bytes_per_point": total_bytes, "saturation": sat, "load_points": points,
+            "server": stats}
+
+
+def run_gpu(args, rank: int, world: int):
+    import torch
+
+    from qz_gb300 import bwt
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    blocks, kinds, desc = make_workload(args.config, args.reads)
+    sizes = [len(b) for b in blocks]
+    N = sum(sizes)
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    host = np.concatenate(blocks)
+    dev = torch.device("cuda", local)
+    d_T = torch.from_numpy(host).to(dev)
+    d_U = torch.empty_like(d_T)
+    d_R = torch.empty_like(d_T)
+    bwt.init()
+    st = bwt.Storage(N, len(blocks))
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    def step():
+        idx = st.encode_device(sizes, d_T.data_ptr(), d_U.data_ptr(), sptr)
+        st.decode_device(sizes, idx, d_U.data_ptr(), d_R.data_ptr(), sptr)
+        return idx
+
+    for kv in args.param:
+        k, v = kv.split("=", 1)
+        st.set_param(k, int(v))
+    # ---- autotuner (before warm-up; not timed)
+    tuned = None
+    if not args.no_autotune:
+        tuned = autotune_storage(st, step, blocks, dev, stream)
+    for _ in range(args.warmup):
+        idx = step()
+    torch.cuda.synchronize(dev)
+    if not torch.equal(d_R, d_T):
+        raise SystemExit("GPU round trip mismatch")
+
+    # ---- per-kernel table and the dominant kernel: one forward + inverse on a
+    # one-lane storage, every launch bracketed by events (nothing else runs on
+    # the GPU meanwhile, so each window is that kernel's own duration); not
+    # part of the timed region
+    peak, peak_kind = load_peak()
+    st1 = one_lane_storage(bwt, N, len(blocks), tuned or st.params(), args.param)
+    i1 = st1.encode_device(sizes, d_T.data_ptr(), d_U.data_ptr(), sptr)
+    st1.decode_device(sizes, i1, d_U.data_ptr(), d_R.data_ptr(), sptr)
+    st1.profile(True)
+    st1.profile_read(reset=True)
+    i1 = st1.encode_device(sizes, d_T.data_ptr(), d_U.data_ptr(), sptr)
+    st1.decode_device(sizes, i1, d_U.data_ptr(), d_R.data_ptr(), sptr)
+    torch.cuda.synchronize(dev)
+    prof_all = st1.profile_read(reset=True)
+    st1.profile(False)
+    st1.close()
+    dominant = prof_all[0]["name"] if prof_all else None
+    kern_total = max(sum(q["ms"] for q in prof_all), 1e-9)
+    kernels = []
+    for p in prof_all:
+        gbs = (p["alg_bytes"] / (p["ms"] / 1e3) / 1e9) if p["ms"] > 0 and p["alg_bytes"] > 0 else None
+        kernels.append({"name": p["name"], "launches": p["launches"], "ms": round(p["ms"], 3),
+                        "share": round(p["ms"] / kern_total, 4), "alg_gb_s": round(gbs, 1) if gbs else None})
+
+    # ---- timed region (device-resident inputs, 818 MB > 126 MB L2); only the
+    # dominant kernel's launches carry events, for the roofline
+    clocks = ClockSampler(local)
+    st.profile(True, only=dominant)
+    st.profile_read(reset=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    time.sleep(0.3)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps + 1)]
+    launches = 0
+    fwd_stats, rounds_active = None, None
+    ev[0].record(stream)
+    for k in range(args.steps):
+        idx = st.encode_device(sizes, d_T.data_ptr(), d_U.data_ptr(), sptr)
+        fwd_stats = st.stats()
+        rounds_active = st.round_counts()
+        launches += fwd_stats["kernel_launches"]
+        ev[2 * k + 1].record(stream)
+        st.decode_device(sizes, idx, d_U.data_ptr(), d_R.data_ptr(), sptr)
+        launches += st.stats()["kernel_launches"]
+        ev[2 * k + 2].record(stream)
+    torch.cuda.synchronize(dev)
+    clk = clocks.stop()
+    if dist:
+        dist.barrier()
+    total_ms = ev[0].elapsed_time(ev[2 * args.steps])
+    fwd_ms = sum(ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(args.steps))
+    inv_ms = sum(ev[2 * k + 1].elapsed_time(ev[2 * k + 2]) for k in range(args.steps))
+    prof_top = st.profile_read(reset=True)
+    st.profile(False)
+    total_ms, fwd_ms, inv_ms = max_over_ranks([total_ms, fwd_ms, inv_ms], dist)
+    value = job_rate(world, N, args.steps, total_ms / 1e3)
+    if not torch.equal(d_R, d_T):
+        raise SystemExit("GPU round trip mismatch in the timed region")
+
+    # ---- roofline of the dominant kernel
+    top = prof_top[0] if prof_top else None
+    roof = None
+    if top:
+        per_launch = top["alg_bytes"] / max(top["launches"], 1)
+        avg_s = top["ms"] / max(top["launches"], 1) / 1e3
+        achieved = per_launch / avg_s / 1e9 if avg_s > 0 else 0.0
+        roof = {"bound": "hbm", "kernel": top["name"], "achieved": round(achieved, 1), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                "alg_bytes_per_launch": int(per_launch), "launches_timed": top["launches"],
+                "how": "algorithmic bytes per launch / event-timed launch duration inside the timed region "
+                       "(the engine's lanes overlap, so a window also holds other lanes' kernels)",
+                "traffic": None}
+        tr = load_traffic().get(top["name"])
+        if isinstance(tr, dict) and tr.get("alg_bytes_per_launch"):
+            # DRAM bytes measured by ncu on a smaller case at the same
+            # sub-batch size, scaled to this launch by its algorithmic bytes
+            ratio = tr["dram_bytes_per_launch"] / tr["alg_bytes_per_launch"]
+            roof["traffic"] = int(ratio * per_launch)
+            roof["traffic_over_alg"] = round(ratio, 3)
+            roof["traffic_source"] = tr.get("source", "profiles/dram_traffic.json")
+        alone = next((p for p in prof_all if p["name"] == top["name"]), None)
+        if alone and alone["launches"] and alone["ms"] > 0:
+            a1 = alone["alg_bytes"] / alone["launches"] / (alone["ms"] / alone["launches"] / 1e3) / 1e9
+            roof["alone"] = {"achieved": round(a1, 1), "frac": round(a1 / peak, 4), "launches": alone["launches"],
+                             "how": "one forward + inverse of the workload on a one-lane storage"}
+
+    # ---- end to end through the host-buffer C ABI (copies inside the timed region)
+    e2e = None
+    if not args.no_e2e:
+        # pinned host buffers, allocated once and reused by every step: the
+        # step's inputs are copied to the device and its outputs back inside
+        # the library calls
+        def pinned(n):
+            return torch.empty(max(n, 1), dtype=torch.uint8, pin_memory=True).numpy()[:n]
+
+        h_in = [pinned(len(b)) for b in blocks]
+        for h, b in zip(h_in, blocks):
+            h[:] = b
+        h_u = [pinned(len(b)) for b in blocks]
+        h_back = [pinned(len(b)) for b in blocks]
+        us, ix = st.encode_batch(h_in, out=h_u)
+        st.decode_batch(h_u, ix, out=h_back)
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            us, ix = st.encode_batch(h_in, out=h_u)
+            back = st.decode_batch(h_u, ix, out=h_back)
+        t1 = time.perf_counter()
+        if not all(np.array_equal(a, b) for a, b in zip(back, blocks)):
+            raise SystemExit("host round trip mismatch")
+        e2e_s = max_over_ranks([t1 - t0], dist)[0]
+        e2e = {"value": round(job_rate(world, N, args.steps, e2e_s), 3), "unit": "MB/s",
+               "h2d_bytes_per_step": 2 * N, "d2h_bytes_per_step": 2 * N,
+               "api": "qzgpu_bwt_encode_batch + qzgpu_bwt_decode_batch (pinned host buffers, reused)"}
+    st.close()
+
+    # ---- CPU baseline on a bounded sample (rank 0, N=1 only), and parity of
+    # the GPU's output of the same blocks against it
+    cpu, parity = None, None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        ids, sample, skinds = cpu_sample(blocks, kinds, cores)
+        te, ti, ous, oidx = time_cpu(sample, cores)
+        cpu = {"value": round(sum(len(b) for b in sample) / (te + ti) / 1e6, 3), "unit": "MB/s", "cores": cores,
+               "kind": "port", "sample": cpu_desc(sample, skinds) + f", one per host thread; forward + inverse; "
+                                                                     f"{CPU_BUILD}",
+               "fwd_mb_s": round(sum(len(b) for b in sample) / te / 1e6, 3),
+               "inv_mb_s": round(sum(len(b) for b in sample) / ti / 1e6, 3), "cpu": cpu_model()}
+        gu = d_U.cpu().numpy()
+        bad = [i for j, i in enumerate(ids)
+               if idx[i] != oidx[j] or not np.array_equal(gu[offs[i]:offs[i + 1]], ous[j])]
+        parity = {"blocks": len(ids), "bytes": int(sum(len(b) for b in sample)), "bit_exact": not bad,
+                  "against": "C oracle (SA-IS), U bytes and primary index of each block from the timed region's "
+                             "last forward call"}
+        if bad:
+            print(json.dumps({"parity": parity, "mismatched_blocks": bad}), file=sys.stderr, flush=True)
+            raise SystemExit(f"GPU output differs from the oracle in blocks {bad}")
+
+    # ---- batched vs plain on the uneven batch, and the serving sweep (rank 0,
+    # one GPU: sub-records beside the headline, not part of its timing)
+    bvp, serving = None, None
+    if rank == 0 and world == 1 and args.config == "chunk":
+        del d_T, d_U, d_R
+        torch.cuda.empty_cache()
+        if not args.no_plain_compare:
+            bvp = batched_vs_plain(args, dev, stream)
+        if not args.no_serve:
+            sv = serve_sweep(120, (0.5, 1.0, 1.5), warmup=1, slots=args.slots)
+            serving = {"workload": "120 requests, Poisson arrivals, 70% forward / 30% inverse, sizes log-uniform "
+                                   "64 KiB-25 MiB, 50% DNA / 30% quality / 20% header",
+                       "saturation_mb_s": sv["saturation"]["mb_s"],
+                       "points": [{k: p[k] for k in ("offered_load", "mb_s", "p50_ms", "p99_ms")}
+                                  for p in sv["load_points"]],
+                       "slots": sv["server"]["slots"], "batches": sv["server"]["batches"]}
+
     if rank == 0:
-        at1 = [p for p in points if p["offered_load"] == 1.0][0]
         line = {
-            "metric": METRIC, "value": sat["mb_s"], "unit": "MB/s", "n_gpus": world, "steps": len(points),
+            "metric": METRIC, "value": round(value, 3), "unit": "MB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded reads of the workload's shape; no public dataset)",
+            "config": workload_config(desc, blocks, world),
+            "tuned": tuned if tuned else None,
+            "fwd_mb_s": round(job_rate(world, N, args.steps, fwd_ms / 1e3), 3),
+            "inv_mb_s": round(job_rate(world, N, args.steps, inv_ms / 1e3), 3),
+            "rounds": fwd_stats["rounds"] if fwd_stats else None,
+            "active_per_round": rounds_active,
+            "gpu_launches": launches,
+            "parity": parity,
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+            "kernels": kernels[:14], "kernels_note": "one forward + inverse on a one-lane storage, events around "
+                                                     "every launch (not the timed region)",
+            "batched_vs_plain": bvp, "serving": serving,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+# --------------------------------------------------------------------------- serving
+
+
+def run_serve(args, rank: int, world: int):
+    import torch
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    from qz_gb300 import bwt
+
+    bwt.init()
+    sv = serve_sweep(args.requests, (0.25, 0.5, 0.75, 1.0, 1.25, 1.5), warmup=args.warmup, slots=args.slots)
+    sat = sv["saturation"]
+    if rank == 0:
+        at1 = [p for p in sv["load_points"] if p["offered_load"] == 1.0][0]
+        line = {
+            "metric": METRIC, "value": sat["mb_s"], "unit": "MB/s", "n_gpus": world, "steps": len(sv["load_points"]),
             "warmup": max(1, args.warmup), "ms_per_step": round(1e3 * sat["wall_s"], 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8",
             "data": "synthetic (seeded reads of the workload's shape; no public dataset)",
-            "config": {"workload": f"serving: {len(reqs)} requests, Poisson arrivals, 70% forward / 30% inverse, "
+            "config": {"workload": f"serving: {sv['requests']} requests, Poisson arrivals, 70% forward / 30% inverse, "
                                    "sizes log-uniform 64 KiB-25 MiB, 50% DNA / 30% quality / 20% header",
-                       "bytes_per_point": total_bytes, "slots": stats["slots"]},
+                       "bytes_per_point": sv["bytes_per_point"], "slots": sv["server"]["slots"]},
             "saturation": sat, "p50_ms_at_saturation_load": at1["p50_ms"], "p99_ms_at_saturation_load": at1["p99_ms"],
-            "load_points": points, "server": stats,
+            "load_points": sv["load_points"], "server": sv["server"],
         }
         print(json.dumps(line), flush=True)
 
@@ -590,10 +717,11 @@ def run_streams(args, rank: int):
 
     from qz_gb300 import bwt
     from qz_gb300 import streams as G
+    from qz_gb300 import synth
 
     if rank != 0:
         return
-    text = synth_chunk_fastq(args.reads)
+    text = synth.chunk_fastq(args.reads)
     n = len(text)
     bwt.init()
     pin = torch.empty(n, dtype=torch.uint8, pin_memory=True).numpy()
@@ -631,12 +759,6 @@ def run_streams(args, rank: int):
     print(json.dumps(line), flush=True)
 
 
-def synth_chunk_fastq(reads: int):
-    from qz_gb300 import synth
-
-    return synth.chunk_fastq(reads)
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -645,22 +767,22 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="chunk", choices=["chunk", "plain", "uneven", "repeat", "ultra", "serve", "streams"])
     ap.add_argument("--requests", type=int, default=300, help="serve: requests per load point")
-    ap.add_argument("--slots", type=int, default=4, help="serve: device slots (bounded by free HBM)")
+    ap.add_argument("--slots", type=int, default=4, help="serve: most device slots (admitted by free HBM)")
     ap.add_argument("--reads", type=int, default=2_500_000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default knobs")
+    ap.add_argument("--no-plain-compare", action="store_true", help="skip the uneven batched-vs-plain sub-record")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving sub-record")
     ap.add_argument("--param", action="append", default=[], metavar="NAME=VALUE",
                     help="set a storage knob (qzgpu_storage_set_param) before timing; repeatable")
-    ap.add_argument("--plain-blocks", action="store_true",
-                    help="also time the plain path: one forward + inverse call per block")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
-        run_reference(args, rank)
+        run_reference(args, rank, world)
     elif args.config == "serve":
         run_serve(args, rank, world)
     elif args.config == "streams":

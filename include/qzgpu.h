@@ -147,6 +147,11 @@ int qzgpu_storage_round_counts(const qzgpu_storage *storage, long long *active, 
  *   "tile_ctas_per_sm"                CTAs per SM of the one-CTA group sort (1..3)
  *   "medium_max"                      longest group sorted by one warp (64..512)
  *   "ruler_stride_log2"               inverse: a ruler every 2^v rows (3..12)
+ *   "big_tile"                        slots per look-back tile of the large-group radix
+ *                                     sort (2048, 4096, 8192)
+ *   "radix_first_bits"                widest first (unstable) radix digit of that sort
+ *                                     (8..11): keys of up to 16 + v bits sort in three
+ *                                     passes, 8 keeps four passes above 24-bit keys
  *   "lookback_test"                   1: failure-detection test (forward calls fail with
  *                                     QZGPU_TIMEOUT through a bounded look-back wait that
  *                                     runs out; no GPU fault); 0: off (default)
@@ -185,14 +190,19 @@ int qzgpu_storage_profile_read(qzgpu_storage *storage, qzgpu_kernel_time *out, i
 
 typedef struct qzgpu_server qzgpu_server;
 
-/* Creates a server with as many slots (device storages of slot_bytes block
- * bytes and slot_blocks blocks each; 0 picks 64 MiB / 256) as fit in
- * hbm_budget_bytes (0: 80% of free HBM), at most max_slots (0: 4).  Each slot
- * has a worker thread and a stream; a free worker batches every waiting
- * request of one direction that fits its slot, in arrival order. */
+/* Creates a server whose slots are device storages of slot_bytes block bytes
+ * and slot_blocks blocks each (0 picks 64 MiB / 256).  It starts with one
+ * slot and admits more on demand, at most max_slots (0: 4): while requests
+ * wait and every slot is busy, one more slot is added when the slots' device
+ * bytes (qzgpu_storage_bytes each) stay within hbm_budget_bytes (0: 80% of
+ * the HBM free at creation) and the free HBM read at that moment covers the
+ * slot plus a 256 MiB reserve; otherwise requests wait for a busy slot.  Each
+ * slot has a worker thread and a stream; a free worker batches every waiting
+ * request of one direction that fits its slot, in arrival order.  Returns
+ * QZGPU_GPU_NOT_ENOUGH_MEMORY when not even one slot fits. */
 int qzgpu_server_create(qzgpu_server **server, long long hbm_budget_bytes, int max_slots, long long slot_bytes,
                         int slot_blocks);
-/* Number of slots the server admitted within its budget. */
+/* Number of slots the server holds now. */
 int qzgpu_server_slots(const qzgpu_server *server);
 /* Queues one block: op QZGPU_OP_FORWARD (in = block, out receives U) or
  * QZGPU_OP_INVERSE (in = U, index = primary index, out receives the block).
@@ -201,13 +211,18 @@ int qzgpu_server_slots(const qzgpu_server *server);
 long long qzgpu_server_submit(qzgpu_server *server, int op, const unsigned char *in, unsigned char *out, int n,
                               int index);
 /* Waits up to timeout_ms (< 0: forever) for a ticket.  Returns 1 when done
- * (status = the request's result code, index_out = primary index of a forward
- * request, latency_ms = submit to completion, queue_ms = submit to start of its
- * batch; the ticket is then released), 0 on timeout, or a negative error. */
+ * (status = the request's own result code, index_out = primary index of a
+ * forward request, latency_ms = submit to completion, queue_ms = submit to
+ * start of its batch; the ticket is then released), 0 on timeout (the ticket
+ * can be waited for again), or a negative error: QZGPU_BAD_PARAMETER for an
+ * unknown or released ticket, or one another thread is already waiting for.
+ * Results are per request: an inverse request whose block cannot be inverted
+ * gets QZGPU_DATA_CORRUPT while the other requests of its batch complete. */
 int qzgpu_server_wait(qzgpu_server *server, long long ticket, int timeout_ms, int *status, int *index_out,
                       double *latency_ms, double *queue_ms);
 /* Counters: completed requests, batches, largest batch, most slots busy at
- * once, requests waiting, slots.  Returns the number of counters. */
+ * once, requests waiting, slots, slot admissions refused for lack of free HBM
+ * (or budget).  Returns the number of counters (7). */
 int qzgpu_server_stats(const qzgpu_server *server, long long *out, int max);
 /* Finishes every queued request, then frees the slots. */
 int qzgpu_server_destroy(qzgpu_server *server);
@@ -227,14 +242,18 @@ int qzgpu_server_destroy(qzgpu_server *server);
  *
  * d_U (input BWT) and d_T (output block) are device pointers of n bytes; they
  * may be the same buffer.  Work runs on `stream` (a cudaStream_t, NULL for the
- * legacy default stream) and the call returns when the result is final.  It
- * calls no cudaMalloc, cudaFree or other allocating routine: its scratch is a
- * fixed 6 MiB device array that every GPU loading this library holds until the
- * process exits.  The first call on a device looks that array's address up
- * (cudaGetSymbolAddress); make that first call before any stream capture.
- * All calls in the process share the array, so calls whose GPU work overlaps
- * (other host threads, other streams) race and must be serialised by the
- * caller.  Returns 0, QZGPU_BLOCK_TOO_LARGE for n > QZGPU_NOALLOC_MAX_BLOCK,
+ * legacy default stream); the call synchronizes that stream and returns when
+ * the result is final.  It calls no cudaMalloc, cudaFree or other allocating
+ * routine: its scratch is a fixed 6 MiB device array that every GPU loading
+ * this library holds until the process exits.  The first call on a device
+ * looks that array's address up (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  That address is not looked up again, so a
+ * cudaDeviceReset in the process is not supported afterwards.  All calls in
+ * the process share the array, so calls whose GPU work overlaps (other host
+ * threads, other streams) race and must be serialised by the caller.  A CUDA
+ * error already pending on the calling thread (from the caller's own work) is
+ * left for the caller and the call returns QZGPU_GPU_ERROR without running.
+ * Returns 0, QZGPU_BLOCK_TOO_LARGE for n > QZGPU_NOALLOC_MAX_BLOCK,
  * QZGPU_DATA_CORRUPT for an index or BWT that cannot be inverted, or another
  * negative code. */
 int qzgpu_bwt_decode_noalloc(const unsigned char *d_U, unsigned char *d_T, int n, int index, void *stream);

@@ -3,8 +3,10 @@
 The library exposes runtime knobs per storage (qzgpu_storage_set_param):
 sub-batch sizes of the forward and inverse lanes, persistent CTAs per SM of
 the look-back radix passes, CTAs per SM of the one-CTA group sort, the longest
-group sorted by one warp (the medium / tile class boundary), and the inverse's
-ruler stride.  The tuner times a forward + inverse of the caller's blocks for
+group sorted by one warp (the medium / tile class boundary), the inverse's
+ruler stride, the look-back tile size of the large-group radix sort and the
+width of its first digit (which decides three or four passes for 25..27-bit
+rank keys).  The tuner times a forward + inverse of the caller's blocks for
 candidate settings (coordinate descent from the defaults, best of `reps`
 timings each) and keeps the fastest.  Results are cached in a JSON file per
 workload signature: GPU name, block-size class and alphabet class.
@@ -25,6 +27,8 @@ SPACE = {
     "tile_ctas_per_sm": [1, 2, 3],
     "medium_max": [64, 128, 256, 512],
     "ruler_stride_log2": [4, 5, 6],
+    "big_tile": [2048, 4096, 8192],
+    "radix_first_bits": [8, 11],
 }
 
 

@@ -115,7 +115,7 @@ class Storage:
                 "alg_bytes": s.alg_bytes}
 
     PARAMS = ("fwd_sub_bytes", "inv_sub_bytes", "big_ctas_per_sm", "tile_ctas_per_sm", "medium_max",
-              "ruler_stride_log2")
+              "ruler_stride_log2", "big_tile", "radix_first_bits")
 
     def set_param(self, name: str, value: int) -> None:
         check(self._lib.qzgpu_storage_set_param(self._h, name.encode(), int(value)), f"set_param({name})")
@@ -225,7 +225,11 @@ class Server:
         self._h = h
         self._bufs = {}
         self._lock = threading.Lock()
-        self.slots = self._lib.qzgpu_server_slots(h)
+
+    @property
+    def slots(self) -> int:
+        """Slots the server holds now (it admits more under load, by free HBM)."""
+        return check(self._lib.qzgpu_server_slots(self._h), "qzgpu_server_slots")
 
     def _submit(self, op: int, data, index: int) -> int:
         src = _as_u8(data)
@@ -262,9 +266,9 @@ class Server:
         return {"out": out[:n], "index": ix.value, "latency_ms": lat.value, "queue_ms": q.value}
 
     def stats(self) -> dict:
-        buf = (ctypes.c_longlong * 6)()
-        check(self._lib.qzgpu_server_stats(self._h, buf, 6), "qzgpu_server_stats")
-        keys = ("completed", "batches", "max_batch", "max_slots_busy", "waiting", "slots")
+        buf = (ctypes.c_longlong * 7)()
+        check(self._lib.qzgpu_server_stats(self._h, buf, 7), "qzgpu_server_stats")
+        keys = ("completed", "batches", "max_batch", "max_slots_busy", "waiting", "slots", "admission_refused")
         return dict(zip(keys, (int(v) for v in buf)))
 
     def close(self) -> None:

@@ -26,6 +26,14 @@ __device__ __forceinline__ void report(DevStatus* st, int code, int where, long 
     }
 }
 
+// A problem that belongs to one block of a batch (an inverse BWT that cannot
+// be inverted): recorded for that block as well, so that a caller batching
+// independent requests can fail the one request and keep the others.
+__device__ __forceinline__ void report_block(DevStatus* st, int* blk_status, int code, int where, int b) {
+    if (blk_status) atomicCAS(blk_status + b, 0, code);
+    report(st, code, where, b);
+}
+
 // True once any kernel has reported a problem: the kernels whose stores are
 // addressed by data that an earlier failure may have left inconsistent (suffix
 // indexes, digit positions) return at entry instead.

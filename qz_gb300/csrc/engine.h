@@ -74,10 +74,13 @@ struct FwdBuffers {
 
 struct InvBuffers {
     int* LF;
-    int* rnext[2];
-    int* rdist[2];
-    int* rlen;
-    int* rrow;      // ruler -> block (for the jump kernel)
+    int* next0;     // per ruler: ruler reached by walking LF (-1: row 0)
+    int* len;       // per ruler: rows walked to reach it
+    int* distF;     // per ruler: rows to row 0 once ranked
+    int* hnext[2];  // per head (every 32nd ruler): next head and rows to it, ping-pong for jumping
+    int* hdist[2];
+    uint8_t* stage; // per ruler: the first-column symbols its walk passes (4 bytes per row of the stride)
+    int* resume;    // per ruler: row where a walk longer than its staging slot stopped staging
     int2* rtiles;   // (block, first ruler) per walk tile
 };
 
@@ -87,6 +90,8 @@ struct Tune {
     int tile_ctas_per_sm = 3;  // CTAs of the one-CTA group sort
     int medium_max = kMedMax;  // longest group sorted by one warp (64..512)
     int ruler_log2 = 5;        // inverse: a ruler every 2^ruler_log2 rows (3..12)
+    int big_tile = 4096;       // slots per look-back tile of the large-group sort (2048, 4096, 8192)
+    int first_digit_max = 11;  // widest first radix digit of the large-group sort (8..11 bits)
     // failure-detection test: in the first stable radix pass the second tile
     // of every group publishes nothing and look-back waits give up after 4096
     // polls, so the tiles after it report QZGPU_TIMEOUT (no GPU fault)
@@ -120,11 +125,13 @@ struct Storage {
     uint8_t* blk_code = nullptr;  // nb * 256 dense symbol codes
     uint32_t* blk_hist = nullptr; // nb * 256 byte counts
     int* blk_idx = nullptr;       // primary indexes out
+    int* blk_status = nullptr;    // per-block result of an inverse (0 or a QZGPU_* code)
     int* blk_aux_rate = nullptr;
     int* blk_aux_off = nullptr;
     int* aux = nullptr;           // auxiliary indexes out
     int2* tiles = nullptr;        // (block, start) per kInitTile tile
     int* blk_tbase = nullptr;     // first tile of each block
+    int* blk_hbase = nullptr;     // inverse: first ruler-list head of each block
 
     FwdBuffers f{};
     InvBuffers v{};
@@ -200,6 +207,8 @@ int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned cha
                cudaStream_t user_stream);
 
 size_t storage_device_bytes(long long cap_bytes, int cap_blocks);
+// Bytes of the inverse's ruler staging for a storage of this capacity.
+size_t inverse_stage_bytes(long long cap_bytes, int cap_blocks);
 int storage_init(Storage* S, long long cap_bytes, int cap_blocks);
 void storage_free(Storage* S);
 
@@ -210,9 +219,12 @@ void storage_free(Storage* S);
 int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d_U, int* idx,
                 const int* aux_rate, int* aux_out, cudaStream_t st);
 
-// Inverse BWT of nb blocks (d_U back to back, device) into d_T.
+// Inverse BWT of nb blocks (d_U back to back, device) into d_T.  block_rc
+// (host, nb entries, may be null) receives each block's own result when the
+// call fails with QZGPU_DATA_CORRUPT: the blocks whose entry is 0 were
+// inverted correctly, the others could not be inverted.
 int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t* d_U, uint8_t* d_T,
-                cudaStream_t st);
+                cudaStream_t st, int* block_rc = nullptr);
 
 int map_cuda_error(cudaError_t e);
 // The library's device (initialised on first use) and its SM count.
@@ -226,8 +238,10 @@ int check_blocks(int nblocks, const int* n, long long* total);
 // until the output pages have been touched).
 int encode_host(Storage* S, int nb, const unsigned char* const* T, unsigned char* const* U, const int* n, int* idx,
                 const int* aux_rate, int* aux_out, const std::function<void()>* before_copy_out = nullptr);
+// block_rc (may be null): per-block results as for inverse_run; when it is
+// given, a call that fails only for some blocks still copies every block out.
 int decode_host(Storage* S, int nb, const unsigned char* const* U, unsigned char* const* T, const int* n,
-                const int* idx, const std::function<void()>* before_copy_out = nullptr);
+                const int* idx, const std::function<void()>* before_copy_out = nullptr, int* block_rc = nullptr);
 
 // Debug mode (environment QZGPU_DEBUG=1): every launch is followed by a
 // stream synchronize and an error check, and failures are logged to stderr.

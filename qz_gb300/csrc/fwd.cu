@@ -1036,7 +1036,7 @@ namespace {
 // Sorts every group (key, W) in place in compact slot space.  hc: host copy
 // of the counters (list lengths, slots per class); A: active slots.
 void sort_groups(Storage* S, const int* hc, int A, const int* d_A, uint32_t* key, int* W, const int* G,
-                 cudaStream_t st, bool small_done) {
+                 cudaStream_t st, bool small_done, int key_bits) {
     FwdBuffers& f = S->f;
     int* cnt = S->counters;
     const int sms = S->sms;
@@ -1049,7 +1049,7 @@ void sort_groups(Storage* S, const int* hc, int A, const int* d_A, uint32_t* key
                   k_sort_small<<<grid_for(A, kThreads, sms * 16), kThreads, 0, st>>>(d_A, G, key, W));
     sort_medium_groups(S, f.list_med, cnt + CNT_MED, hc[CNT_MED], hc[CNT_MED_ELEMS], key, W, key, W, st);
     sort_tile_groups(S, f.list_tile, cnt + CNT_TILE, hc[CNT_TILE], hc[CNT_TILE_ELEMS], key, W, key, W, st);
-    sort_big_groups(S, f.list_large, cnt + CNT_LARGE, hc[CNT_LARGE], hc[CNT_LARGE_ELEMS], key, W, st);
+    sort_big_groups(S, f.list_large, cnt + CNT_LARGE, hc[CNT_LARGE], hc[CNT_LARGE_ELEMS], key, W, key_bits, st);
 }
 
 }  // namespace
@@ -1175,7 +1175,8 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
     int act = CNT_ACTIVE;  // counter slot holding the current active count
     GatherArgs ga{f.R, S->blk_off, nb, S->blk_K, -1};
     // ---- initial sort (groups = blocks)
-    sort_groups(S, cnt0, (int)N, S->counters + act, f.key, f.W[0], f.G[0], st, false);
+    // initial keys: up to 32 bits of packed symbols
+    sort_groups(S, cnt0, (int)N, S->counters + act, f.key, f.W[0], f.G[0], st, false, 32);
     if (dump) {
         dump_array("sorted_key", f.key, 4 * N, st);
         dump_array("sorted_W", f.W[0], 4 * N, st);
@@ -1236,6 +1237,11 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
     add_round(S, 0, N);
 
     int* hcnt = S->pin_rd;
+    // rank keys R[x+h] + h + 1 (R < N, h <= n_b) and end keys (<= n_b): below N + max n_b
+    int nmax = 0;
+    for (int b = 0; b < nb; ++b) nmax = std::max(nmax, n[b]);
+    int rank_key_bits = 1;
+    while (rank_key_bits < 32 && (1ll << rank_key_bits) <= N + nmax) ++rank_key_bits;
     int round = 0;
     long long A_prev = N;
     int last_mode = kRankNone;
@@ -1291,7 +1297,9 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
         QZ_LAUNCH(S, st, "k_sort_straddle", nruns,
                   k_sort_straddle<<<grid_for(nruns, kWarps, S->sms * 16), kThreads, 0, st>>>(
                       S->counters + act, f.G[cur], f.key, f.W[cur], f.straddle));
-        sort_groups(S, hcnt, A, S->counters + act, f.key, f.W[cur], f.G[cur], st, true);
+        // round 0 gathers 32-bit text keys; later rounds rank keys below N + max n_b
+        sort_groups(S, hcnt, A, S->counters + act, f.key, f.W[cur], f.G[cur], st, true,
+                    round == 0 ? 32 : rank_key_bits);
         if (dump) {
             dump_array("rsorted_key", f.key, 4 * (size_t)A, st);
             dump_array("rsorted_W", f.W[cur], 4 * (size_t)A, st);

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "radix.cuh"
 
 namespace qz {
 
@@ -143,7 +144,9 @@ Caps caps_for(long long cap_bytes, int cap_blocks) {
     c.med = c.N / (kSmallMax + 1) + 1;
     c.tile = c.N / 65 + 2;  // medium_max may be tuned down to 64
     c.large = c.N / (kOT + 1) + 2;
-    c.big_tiles = 2 * (c.N / kOT) + 2;
+    // look-back tiles of the large-group sort at its smallest tile (2048):
+    // ceil(len / 2048) summed over groups longer than kOT
+    c.big_tiles = c.N / 2048 + c.N / (kOT + 1) + 4;
     c.rulers = (c.N >> kMinStrideLog2) + c.nb + 1;
     c.rtiles = c.rulers / kThreads + c.nb + 1;
     c.aux = 64 * c.nb + 64;
@@ -168,9 +171,11 @@ size_t layout(Storage* S, char* base, const Caps& c) {
     s->blk_code = cv.take<uint8_t>(256 * c.nb);
     s->blk_hist = cv.take<uint32_t>(256 * c.nb);
     s->blk_idx = cv.take<int>(c.nb + 1);
+    s->blk_status = cv.take<int>(c.nb + 1);
     s->blk_aux_rate = cv.take<int>(c.nb + 1);
     s->blk_aux_off = cv.take<int>(c.nb + 1);
     s->blk_tbase = cv.take<int>(c.nb + 1);
+    s->blk_hbase = cv.take<int>(c.nb + 1);
     s->aux = cv.take<int>(c.aux);
     s->tiles = cv.take<int2>(c.init_tiles);
     size_t shared_start = cv.off;
@@ -190,7 +195,7 @@ size_t layout(Storage* S, char* base, const Caps& c) {
     f.straddle = cv.take<uint8_t>(c.N / 32 + 64);
     f.list_tile = cv.take<int2>(c.tile);
     f.list_large = cv.take<int2>(c.large);
-    f.h4 = cv.take<uint32_t>(1024 * c.large);
+    f.h4 = cv.take<uint32_t>(big_hist_words() * c.large);
     f.status64 = cv.take<unsigned long long>(256 * c.big_tiles);
     f.gmask = cv.take<uint32_t>(c.large + 1);
     f.ltc = cv.take<uint32_t>(c.large + 1);
@@ -210,12 +215,16 @@ size_t layout(Storage* S, char* base, const Caps& c) {
     cv.off = shared_start;
     InvBuffers& v = s->v;
     v.LF = cv.take<int>(c.N + c.nb + 1);
+    v.next0 = cv.take<int>(c.rulers);
+    v.len = cv.take<int>(c.rulers);
+    v.distF = cv.take<int>(c.rulers);
+    const size_t heads = c.rulers / 32 + c.nb + 1;
     for (int i = 0; i < 2; ++i) {
-        v.rnext[i] = cv.take<int>(c.rulers);
-        v.rdist[i] = cv.take<int>(c.rulers);
+        v.hnext[i] = cv.take<int>(heads);
+        v.hdist[i] = cv.take<int>(heads);
     }
-    v.rlen = cv.take<int>(c.rulers);
-    v.rrow = nullptr;
+    v.stage = cv.take<uint8_t>(inverse_stage_bytes((long long)c.N, (int)c.nb));
+    v.resume = cv.take<int>(c.rulers);
     v.rtiles = cv.take<int2>(c.rtiles);
     return std::max(fwd_end, cv.off) + kAlign;
 }
@@ -403,7 +412,7 @@ int encode_host(Storage* S, int nb, const unsigned char* const* T, unsigned char
 }
 
 int decode_host(Storage* S, int nb, const unsigned char* const* U, unsigned char* const* T, const int* n,
-                const int* idx, const std::function<void()>* before_copy_out) {
+                const int* idx, const std::function<void()>* before_copy_out, int* block_rc) {
     cudaError_t e = cudaSetDevice(S->device);
     if (e != cudaSuccess) return map_cuda_error(e);
     long long off = 0;
@@ -414,19 +423,20 @@ int decode_host(Storage* S, int nb, const unsigned char* const* U, unsigned char
         }
         off += n[b];
     }
-    int rc = inverse_run(S, nb, n, idx, S->U, S->T, S->stream);
-    if (rc) return rc;
+    const int rc = inverse_run(S, nb, n, idx, S->U, S->T, S->stream, block_rc);
+    // a failure of some blocks only (block_rc says which): the others are final
+    if (rc && !(rc == QZGPU_DATA_CORRUPT && block_rc)) return rc;
     if (before_copy_out) (*before_copy_out)();
     off = 0;
     for (int b = 0; b < nb; ++b) {
-        if (n[b] > 0) {
+        if (n[b] > 0 && !(block_rc && block_rc[b])) {
             e = cudaMemcpyAsync(T[b], S->T + off, (size_t)n[b], cudaMemcpyDeviceToHost, S->stream);
             if (e != cudaSuccess) return map_cuda_error(e);
         }
         off += n[b];
     }
     e = cudaStreamSynchronize(S->stream);
-    return map_cuda_error(e);
+    return e != cudaSuccess ? map_cuda_error(e) : rc;
 }
 
 int device_info(int* device, int* sms) {
@@ -637,6 +647,12 @@ int qzgpu_storage_set_param(qzgpu_storage* storage, const char* name, long long 
     } else if (k == "ruler_stride_log2") {
         if (value < 3 || value > 12) return QZGPU_BAD_PARAMETER;
         each([&](Tune& t) { t.ruler_log2 = (int)value; });
+    } else if (k == "big_tile") {
+        if (value != 2048 && value != 4096 && value != 8192) return QZGPU_BAD_PARAMETER;
+        each([&](Tune& t) { t.big_tile = (int)value; });
+    } else if (k == "radix_first_bits") {
+        if (value < 8 || value > 11) return QZGPU_BAD_PARAMETER;
+        each([&](Tune& t) { t.first_digit_max = (int)value; });
     } else if (k == "lookback_test") {
         if (value < 0 || value > 1) return QZGPU_BAD_PARAMETER;
         each([&](Tune& t) { t.lookback_test = (int)value; });
@@ -656,6 +672,8 @@ long long qzgpu_storage_get_param(const qzgpu_storage* storage, const char* name
     if (k == "tile_ctas_per_sm") return t.tile_ctas_per_sm;
     if (k == "medium_max") return t.medium_max;
     if (k == "ruler_stride_log2") return t.ruler_log2;
+    if (k == "big_tile") return t.big_tile;
+    if (k == "radix_first_bits") return t.first_digit_max;
     if (k == "lookback_test") return t.lookback_test;
     if (k == "lanes") return (long long)storage->lanes.size();
     return QZGPU_BAD_PARAMETER;

@@ -4,19 +4,21 @@
 //   * groups of up to kOT slots: one CTA sorts the whole group in shared
 //     memory (8-bit LSD passes, digits constant across the group skipped),
 //     reading and writing global memory once;
-//   * longer groups: one 8-bit LSD pass per launch over 4096-slot tiles
-//     ("onesweep").  One histogram kernel gives each group's digit totals for
-//     all four passes and marks the passes whose digit is not constant in the
-//     group; the group runs only those.  Pass 0 needs no stability (equal keys
-//     may leave in any order): tiles rank with shared atomics and reserve their
-//     output with one atomic per digit on the group's cursor.  The later passes
-//     are stable: each tile takes a ticket in order, publishes its digit
-//     counts, and looks back over the tiles before it in the same group for
-//     its exclusive prefix (decoupled look-back), then scatters through shared
-//     memory so that each digit's run leaves as coalesced writes.  A tile
-//     loads its keys to registers and its values to shared memory (4-byte
-//     cp.async) together, and finds its group through the tile table the
-//     histogram kernel writes.
+//   * longer groups: one LSD pass per launch over tiles of 2048, 4096 or
+//     8192 slots ("onesweep").  Pass 0 takes the low 8..11 bits, passes 1..3
+//     8 bits each, so keys of up to 27 bits (the rank keys of every round
+//     after the first) sort in three passes.  One histogram kernel gives each
+//     group's digit totals for all passes and marks the passes whose digit is
+//     not constant in the group; the group runs only those.  Pass 0 needs no
+//     stability (equal keys may leave in any order): tiles rank with shared
+//     atomics and reserve their output with one atomic per digit on the
+//     group's cursor.  The later passes are stable: each tile takes a ticket in
+//     order, publishes its digit counts, and looks back over the tiles before
+//     it in the same group for its exclusive prefix (decoupled look-back), then
+//     scatters through shared memory so that each digit's run leaves as
+//     coalesced writes.  A tile loads its keys to registers and its values to
+//     shared memory (4-byte cp.async) together, and finds its group through
+//     the tile table the histogram kernel writes.
 //
 // Look-back waits are bounded: a tile only waits on tiles that took earlier
 // tickets, which publish their counts before they wait themselves; a wait that
@@ -31,7 +33,6 @@
 namespace qz {
 
 constexpr int kOItems = kOT / kThreads;   // 16 slots per thread
-constexpr int kOWarpSpan = kOT / kWarps;  // 512 contiguous slots per warp
 constexpr unsigned long long kFlagAgg = 1ull << 32;
 constexpr unsigned long long kFlagInc = 2ull << 32;
 constexpr unsigned kSpinLimit = 1u << 24;
@@ -158,14 +159,26 @@ __global__ void __launch_bounds__(kThreads) k_tile_sort(const int2* __restrict__
 }
 
 // ------------------------------------------------------------------ multi-tile groups
+//
+// Digit layout of one large-group sort: pass 0 takes the low w0 bits (8..11)
+// and is unstable, so its ranking needs only shared-memory counters; passes
+// 1..3 take 8 bits each above it.  Keys of at most w0 + 16 bits (the rank keys
+// of a 25 MiB block need 26) therefore sort in three passes.  Per group the
+// digit counts sit in kH4 words: pass 0's 2^w0 counts, then 256 per later pass.
+// The look-back tile holds TILE slots (2048, 4096 or 8192; a tuning knob).
+constexpr int kH0 = 2048;            // pass-0 bins at most (11 bits)
+constexpr int kH4 = kH0 + 3 * 256;   // digit-count words per group
+
+__device__ __forceinline__ int digit_shift(int pass, int w0) { return pass == 0 ? 0 : w0 + 8 * (pass - 1); }
+__device__ __forceinline__ int h4_row(int pass) { return pass == 0 ? 0 : kH0 + 256 * (pass - 1); }
 
 __global__ void __launch_bounds__(kThreads) k_big_prep(const int2* __restrict__ list, const int* __restrict__ d_count,
                                                        uint32_t* __restrict__ tcount, uint32_t* __restrict__ lens,
-                                                       uint32_t* __restrict__ gmask) {
+                                                       uint32_t* __restrict__ gmask, int tile) {
     int cnt = *d_count;
     for (int i = blockIdx.x * kThreads + threadIdx.x; i < cnt; i += gridDim.x * kThreads) {
         int len = list[i].y;
-        tcount[i] = (uint32_t)((len + kOT - 1) / kOT);
+        tcount[i] = (uint32_t)((len + tile - 1) / tile);
         lens[i] = (uint32_t)len;
         gmask[i] = 0;
     }
@@ -182,7 +195,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_big_plan(const int2* __restric
                                                            const int* __restrict__ d_count,
                                                            uint32_t* __restrict__ tbase, uint32_t* __restrict__ wbase,
                                                            uint32_t* __restrict__ gmask,
-                                                           int* __restrict__ total_tiles) {
+                                                           int* __restrict__ total_tiles, int tile) {
     __shared__ uint32_t sht[kPlanThreads / 32 + 1], shw[kPlanThreads / 32 + 1];
     const int cnt = *d_count;
     // each thread owns a contiguous run of groups: its loads are issued
@@ -193,7 +206,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_big_plan(const int2* __restric
 #pragma unroll 8
     for (int i = i0; i < i1; ++i) {
         const uint32_t len = (uint32_t)__ldg(&list[i].y);
-        st += (len + kOT - 1) / kOT;
+        st += (len + tile - 1) / tile;
         sw += len;
     }
     const unsigned ln = lane_id(), wp = warp_id();
@@ -218,7 +231,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_big_plan(const int2* __restric
         tbase[i] = et;
         wbase[i] = ew;
         gmask[i] = 0;
-        et += (len + kOT - 1) / kOT;
+        et += (len + tile - 1) / tile;
         ew += len;
     }
 }
@@ -233,60 +246,91 @@ __device__ __forceinline__ int big_seg_of_tile(const uint32_t* __restrict__ tbas
     return lo;
 }
 
-// Digit counts of all four passes per group (order-independent), by tile.
+// Digit counts of all passes per group (order-independent), by tile.
+template <int TILE>
 __global__ void __launch_bounds__(kThreads) k_big_hist(BigArgs a, const uint32_t* __restrict__ key,
-                                                       uint32_t* __restrict__ h4) {
-    __shared__ uint32_t h[4][256];
+                                                       uint32_t* __restrict__ h4, int w0) {
+    constexpr int IT = TILE / kThreads;
+    __shared__ uint32_t h0[kH0];
+    __shared__ uint32_t h[3][256];
     __shared__ int s_seg;
+    const int nb0 = 1 << w0;
+    const uint32_t m0 = (uint32_t)nb0 - 1u;
     int TT = *a.ntiles, nseg = *a.nseg;
     for (int tau = blockIdx.x; tau < TT; tau += gridDim.x) {
         if (threadIdx.x == 0) {
             s_seg = big_seg_of_tile(a.tbase, nseg, (uint32_t)tau);
             a.tseg[tau] = (uint32_t)s_seg;  // the passes read it in one load
         }
+        for (int i = threadIdx.x; i < nb0; i += kThreads) h0[i] = 0;
 #pragma unroll
-        for (int p = 0; p < 4; ++p) h[p][threadIdx.x] = 0;
+        for (int p = 0; p < 3; ++p) h[p][threadIdx.x] = 0;
         __syncthreads();
         int s = s_seg;
         int2 d = a.list[s];
         int j = tau - (int)a.tbase[s];
-        int base = d.x + j * kOT;
-        int cnt = min(kOT, d.y - j * kOT);
-        uint32_t kr[kOItems];
+        int base = d.x + j * TILE;
+        int cnt = min(TILE, d.y - j * TILE);
+        uint32_t kr[IT];
 #pragma unroll
-        for (int it = 0; it < kOItems; ++it) {
+        for (int it = 0; it < IT; ++it) {
             int i = it * kThreads + threadIdx.x;
             kr[it] = i < cnt ? __ldg(key + base + i) : 0u;
         }
 #pragma unroll
-        for (int it = 0; it < kOItems; ++it) {
+        for (int it = 0; it < IT; ++it) {
             if (it * kThreads + (int)threadIdx.x < cnt) {
+                atomicAdd(&h0[kr[it] & m0], 1u);
 #pragma unroll
-                for (int p = 0; p < 4; ++p) atomicAdd(&h[p][(kr[it] >> (8 * p)) & 255u], 1u);
+                for (int p = 0; p < 3; ++p) atomicAdd(&h[p][(kr[it] >> (w0 + 8 * p)) & 255u], 1u);
             }
         }
         __syncthreads();
+        uint32_t* g = h4 + (size_t)s * kH4;
+        for (int i = threadIdx.x; i < nb0; i += kThreads) {
+            uint32_t v = h0[i];
+            if (v) atomicAdd(&g[i], v);
+        }
 #pragma unroll
-        for (int p = 0; p < 4; ++p) {
+        for (int p = 0; p < 3; ++p) {
             uint32_t v = h[p][threadIdx.x];
-            if (v) atomicAdd(&h4[((size_t)s * 4 + p) * 256 + threadIdx.x], v);
+            if (v) atomicAdd(&g[kH0 + 256 * p + threadIdx.x], v);
         }
         __syncthreads();
     }
 }
 
-// Per group and pass: exclusive prefix over the 256 digits (in place), and
+// Per group and pass: exclusive prefix over the pass's digits (in place), and
 // the pass is marked needed unless one digit holds the whole group.
-__global__ void __launch_bounds__(kThreads) k_big_bases(BigArgs a, uint32_t* __restrict__ h4) {
+__global__ void __launch_bounds__(kThreads) k_big_bases(BigArgs a, uint32_t* __restrict__ h4, int w0) {
     __shared__ uint32_t sh[kWarps + 1];
-    int n = *a.nseg * 4;
+    const int n = *a.nseg * 4;
+    const int per0 = (1 << w0) / kThreads;  // pass-0 digits per thread (1..8)
     for (int r = blockIdx.x; r < n; r += gridDim.x) {
-        uint32_t v = h4[(size_t)r * 256 + threadIdx.x];
-        const uint32_t len = (uint32_t)a.list[r >> 2].y;
-        const bool whole = __syncthreads_or(v == len);
+        const int s = r >> 2, p = r & 3;
+        const uint32_t len = (uint32_t)a.list[s].y;
+        uint32_t* row = h4 + (size_t)s * kH4 + h4_row(p);
+        const int per = p == 0 ? per0 : 1;
+        uint32_t v[kH0 / kThreads];
+        uint32_t sum = 0;
+        bool whole = false;
+#pragma unroll
+        for (int i = 0; i < kH0 / kThreads; ++i) {
+            v[i] = i < per ? row[threadIdx.x * per + i] : 0u;
+            sum += v[i];
+            whole |= v[i] == len;
+        }
+        whole = __syncthreads_or(whole);
         uint32_t tot;
-        h4[(size_t)r * 256 + threadIdx.x] = block_excl_sum(v, sh, &tot);
-        if (threadIdx.x == 0 && !whole) atomicOr(&a.gmask[r >> 2], 1u << (r & 3));
+        uint32_t ex = block_excl_sum(sum, sh, &tot);
+#pragma unroll
+        for (int i = 0; i < kH0 / kThreads; ++i) {
+            if (i < per) {
+                row[threadIdx.x * per + i] = ex;
+                ex += v[i];
+            }
+        }
+        if (threadIdx.x == 0 && !whole) atomicOr(&a.gmask[s], 1u << p);
     }
 }
 
@@ -320,24 +364,32 @@ __device__ __forceinline__ BigRoute big_route(const BigBuffers& bb, const int2 d
     return r;
 }
 
-// Pass 0 (bits 0..7).  Equal keys may leave a group sort in any order (the
-// split gives them one rank), so this pass needs no stability: a tile ranks its
-// slots with shared-memory atomics and reserves each digit's output range with
-// one atomic on the group's digit cursor (its pass-0 base row), so it neither
-// matches nor looks back.
-__global__ void __launch_bounds__(kThreads, 3) k_big_pass0(BigArgs a, uint32_t* __restrict__ h4, BigBuffers bb) {
-    __shared__ uint32_t skey[kOT];
-    __shared__ int sval[kOT];
-    __shared__ int vst[kOT];  // the tile's values in slot order (asynchronous copies)
-    __shared__ uint32_t cnt[256];
-    __shared__ uint32_t gb[256];
+template <int TILE>
+constexpr int big_min_ctas() { return TILE >= 8192 ? 2 : 3; }
+
+// Pass 0 (the low w0 bits).  Equal keys may leave a group sort in any order
+// (the split gives them one rank), so this pass needs no stability: a tile
+// ranks its slots with shared-memory atomics and reserves each digit's output
+// range with one atomic on the group's digit cursor (its pass-0 base row), so
+// it neither matches nor looks back.
+template <int TILE>
+__global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass0(BigArgs a, uint32_t* __restrict__ h4,
+                                                                              BigBuffers bb, int w0) {
+    constexpr int IT = TILE / kThreads, WSPAN = TILE / kWarps;
+    __shared__ uint32_t skey[TILE];
+    __shared__ int sval[TILE];
+    __shared__ int vst[TILE];  // the tile's values in slot order (asynchronous copies)
+    __shared__ uint32_t cnt[kH0];
+    __shared__ uint32_t gb[kH0];
     __shared__ uint32_t sh[kWarps + 1];
     __shared__ int s_seg;
     const unsigned w = warp_id(), ln = lane_id();
+    const int nb0 = 1 << w0, per = nb0 / kThreads;
+    const uint32_t m0 = (uint32_t)nb0 - 1u;
     const int TT = *a.ntiles;
     for (int tau = blockIdx.x; tau < TT; tau += gridDim.x) {
         if (threadIdx.x == 0) s_seg = (int)a.tseg[tau];
-        cnt[threadIdx.x] = 0;
+        for (int i = threadIdx.x; i < nb0; i += kThreads) cnt[i] = 0;
         __syncthreads();
         const int s = s_seg;
         const uint32_t m = big_passes(a.gmask[s]);
@@ -353,37 +405,52 @@ __global__ void __launch_bounds__(kThreads, 3) k_big_pass0(BigArgs a, uint32_t* 
         const int* sv = rt.sv;
         uint32_t* dk = rt.dk;
         int* dv = rt.dv;
-        const int src = j * kOT;
-        const int n = min(kOT, d.y - j * kOT);
-        uint32_t kr[kOItems], rk[kOItems];
+        const int src = j * TILE;
+        const int n = min(TILE, d.y - j * TILE);
+        uint32_t kr[IT], rk[IT];
         // keys to registers and values to shared memory, all in flight at once
 #pragma unroll
-        for (int it = 0; it < kOItems; ++it) {
-            int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
+        for (int it = 0; it < IT; ++it) {
+            int i = (int)w * WSPAN + it * 32 + (int)ln;
             kr[it] = i < n ? __ldcs(sk + src + i) : 0u;
             if (i < n) cp_async4(vst + i, sv + src + i);
         }
 #pragma unroll
-        for (int it = 0; it < kOItems; ++it) {
-            int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
-            rk[it] = i < n ? atomicAdd(&cnt[kr[it] & 255u], 1u) : 0u;
+        for (int it = 0; it < IT; ++it) {
+            int i = (int)w * WSPAN + it * 32 + (int)ln;
+            rk[it] = i < n ? atomicAdd(&cnt[kr[it] & m0], 1u) : 0u;
         }
         __syncthreads();
         {
-            const uint32_t c = cnt[threadIdx.x];
-            const uint32_t base = c ? atomicAdd(&h4[(size_t)s * 1024 + threadIdx.x], c) : 0u;
+            // this thread's run of `per` consecutive digits: tile offsets and
+            // the group's output cursor for each
+            uint32_t c[kH0 / kThreads];
+            uint32_t sum = 0;
+#pragma unroll
+            for (int i = 0; i < kH0 / kThreads; ++i) {
+                c[i] = i < per ? cnt[threadIdx.x * per + i] : 0u;
+                sum += c[i];
+            }
             uint32_t tot;
-            const uint32_t off = block_excl_sum(c, sh, &tot);
-            cnt[threadIdx.x] = off;
-            gb[threadIdx.x] = base - off;
+            uint32_t off = block_excl_sum(sum, sh, &tot);
+#pragma unroll
+            for (int i = 0; i < kH0 / kThreads; ++i) {
+                if (i < per) {
+                    const int dg = threadIdx.x * per + i;
+                    const uint32_t base = c[i] ? atomicAdd(&h4[(size_t)s * kH4 + dg], c[i]) : 0u;
+                    cnt[dg] = off;
+                    gb[dg] = base - off;
+                    off += c[i];
+                }
+            }
         }
         cp_async_wait_all();  // each thread reads back only the values it copied
         __syncthreads();
 #pragma unroll
-        for (int it = 0; it < kOItems; ++it) {
-            int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
+        for (int it = 0; it < IT; ++it) {
+            int i = (int)w * WSPAN + it * 32 + (int)ln;
             if (i < n) {
-                uint32_t lp = cnt[kr[it] & 255u] + rk[it];
+                uint32_t lp = cnt[kr[it] & m0] + rk[it];
                 skey[lp] = kr[it];
                 sval[lp] = vst[i];
             }
@@ -391,7 +458,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_big_pass0(BigArgs a, uint32_t* 
         __syncthreads();
         for (int i = threadIdx.x; i < n; i += kThreads) {
             uint32_t kv = skey[i];
-            uint32_t dst = gb[kv & 255u] + (uint32_t)i;
+            uint32_t dst = gb[kv & m0] + (uint32_t)i;
             dk[dst] = kv;
             dv[dst] = sval[i];
         }
@@ -399,14 +466,15 @@ __global__ void __launch_bounds__(kThreads, 3) k_big_pass0(BigArgs a, uint32_t* 
     }
 }
 
-// One stable 8-bit pass with decoupled look-back.
-__global__ void __launch_bounds__(kThreads, 3) k_big_pass(BigArgs a, const uint32_t* __restrict__ h4, int pass,
-                                                          unsigned epoch, BigBuffers bb, unsigned long long* status,
-                                                          unsigned* ticket, DevStatus* st, unsigned spin_limit,
-                                                          int silent_tile) {
-    __shared__ uint32_t skey[kOT];
-    __shared__ int sval[kOT];
-    __shared__ int vst[kOT];  // the tile's values in slot order (asynchronous copies)
+// One stable 8-bit pass (1..3) with decoupled look-back.
+template <int TILE>
+__global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass(
+    BigArgs a, const uint32_t* __restrict__ h4, int pass, int w0, unsigned epoch, BigBuffers bb,
+    unsigned long long* status, unsigned* ticket, DevStatus* st, unsigned spin_limit, int silent_tile) {
+    constexpr int IT = TILE / kThreads, WSPAN = TILE / kWarps;
+    __shared__ uint32_t skey[TILE];
+    __shared__ int sval[TILE];
+    __shared__ int vst[TILE];  // the tile's values in slot order (asynchronous copies)
     __shared__ uint32_t wcnt[kWarps][256];
     __shared__ uint32_t dig_off[256];
     __shared__ uint32_t gbase[256];
@@ -414,7 +482,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_big_pass(BigArgs a, const uint3
     __shared__ int s_tau, s_seg;
     const unsigned w = warp_id(), ln = lane_id();
     const unsigned lt_mask = (1u << ln) - 1u;
-    const int shift = 8 * pass;
+    const int shift = digit_shift(pass, w0);
     const unsigned long long ep = (unsigned long long)epoch << 34;
     // an earlier pass that failed leaves keys whose digits no longer match the
     // group histograms, so the positions below would not stay in the group
@@ -445,20 +513,20 @@ __global__ void __launch_bounds__(kThreads, 3) k_big_pass(BigArgs a, const uint3
         const int* srcv = rt.sv;
         uint32_t* dstk = rt.dk;
         int* dstv = rt.dv;
-        int srcbase = j * kOT;
-        int cnt = min(kOT, d.y - j * kOT);
-        uint32_t rk[kOItems], kr[kOItems];
+        int srcbase = j * TILE;
+        int cnt = min(TILE, d.y - j * TILE);
+        uint32_t rk[IT], kr[IT];
         // all of the tile's keys (to registers) and values (to shared memory)
         // in flight at once, then the ranking
 #pragma unroll
-        for (int it = 0; it < kOItems; ++it) {
-            int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
+        for (int it = 0; it < IT; ++it) {
+            int i = (int)w * WSPAN + it * 32 + (int)ln;
             kr[it] = i < cnt ? __ldg(srck + srcbase + i) : 0u;
             if (i < cnt) cp_async4(vst + i, srcv + srcbase + i);
         }
 #pragma unroll
-        for (int it = 0; it < kOItems; ++it) {
-            int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
+        for (int it = 0; it < IT; ++it) {
+            int i = (int)w * WSPAN + it * 32 + (int)ln;
             bool valid = i < cnt;
             uint32_t kv = kr[it];
             unsigned dg = valid ? (kv >> shift) & 255u : 256u;
@@ -511,13 +579,13 @@ __global__ void __launch_bounds__(kThreads, 3) k_big_pass(BigArgs a, const uint3
             }
             uint32_t tot;
             dig_off[dg] = block_excl_sum(run, sh, &tot);
-            gbase[dg] = h4[((size_t)s * 4 + pass) * 256 + dg] + excl;
+            gbase[dg] = h4[(size_t)s * kH4 + h4_row(pass) + dg] + excl;
         }
         cp_async_wait_all();  // each thread reads back only the values it copied
         __syncthreads();
 #pragma unroll
-        for (int it = 0; it < kOItems; ++it) {
-            int i = (int)w * kOWarpSpan + it * 32 + (int)ln;
+        for (int it = 0; it < IT; ++it) {
+            int i = (int)w * WSPAN + it * 32 + (int)ln;
             if (i < cnt) {
                 uint32_t kv = kr[it];
                 unsigned dg = (kv >> shift) & 255u;
@@ -550,6 +618,7 @@ int grid_cap(long long work, int per_cta, int cap) {
 }  // namespace
 
 size_t tile_sort_smem() { return (size_t)kOT * 16 + sizeof(uint32_t) * kWarps * 256; }
+size_t big_hist_words() { return kH4; }
 
 void sort_tile_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
                       const uint32_t* skey, const int* sval, uint32_t* key, int* val, cudaStream_t st) {
@@ -567,55 +636,78 @@ void sort_tile_groups(Storage* S, const int2* list, const int* d_count, int host
 namespace {
 
 // Tile bases (and the total tile count) per listed group, cleared digit masks.
-void big_plan(Storage* S, const int2* list, const int* d_count, int host_count, cudaStream_t st) {
+void big_plan(Storage* S, const int2* list, const int* d_count, int host_count, int tile, cudaStream_t st) {
     FwdBuffers& f = S->f;
     int* cnt = S->counters;
     if (host_count <= kPlanMaxGroups) {
         QZ_LAUNCH(S, st, "k_big_plan", 20ll * host_count,
                   k_big_plan<<<1, kPlanThreads, 0, st>>>(list, d_count, f.ltbase, f.lwbase, f.gmask,
-                                                         cnt + CNT_LTILES));
+                                                         cnt + CNT_LTILES, tile));
     } else {
         QZ_LAUNCH(S, st, "k_big_prep", 20ll * host_count,
                   k_big_prep<<<grid_cap(host_count, kThreads, S->sms * 4), kThreads, 0, st>>>(list, d_count, f.ltc,
-                                                                                             f.llen, f.gmask));
+                                                                                             f.llen, f.gmask, tile));
         scan_exclusive(S, f.ltc, f.ltbase, 0, d_count, (uint32_t*)(cnt + CNT_LTILES), st);
         scan_exclusive(S, f.llen, f.lwbase, 0, d_count, nullptr, st);
     }
 }
 
-}  // namespace
+// Width of pass 0's digit for keys of key_bits bits: wide enough that three
+// 8-bit passes above it cover the key, up to the tuned maximum; 8 otherwise.
+int first_digit_bits(int key_bits, int max_bits) {
+    if (key_bits > 24 && key_bits <= 16 + max_bits) return key_bits - 16;
+    return 8;
+}
 
-void sort_big_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
-                     uint32_t* key, int* val, cudaStream_t st) {
-    if (host_count <= 0) return;
+template <int TILE>
+void big_sort_run(Storage* S, const BigArgs& a, const BigBuffers& bb, uint32_t* h4, int host_count,
+                  long long elems, int w0, int npass, cudaStream_t st) {
     FwdBuffers& f = S->f;
     int* cnt = S->counters;
     const int sms = S->sms;
-    big_plan(S, list, d_count, host_count, st);
-    BigArgs a{list, d_count, f.ltbase, f.lwbase, cnt + CNT_LTILES, f.gmask, f.tseg};
-    BigBuffers bb{key, val, {f.wsk[0], f.wsk[1]}, {f.wsv[0], f.wsv[1]}};
-    uint32_t* h4 = f.h4;
-    cudaMemsetAsync(h4, 0, sizeof(uint32_t) * 1024 * (size_t)host_count, st);
-    int grid = sms * 4;
-    QZ_LAUNCH(S, st, "k_big_hist", 4 * elems, k_big_hist<<<grid, kThreads, 0, st>>>(a, key, h4));
-    QZ_LAUNCH(S, st, "k_big_bases", 4096ll * host_count,
-              k_big_bases<<<grid_cap(4ll * host_count, 1, sms * 8), kThreads, 0, st>>>(a, h4));
+    const int grid = sms * 4;
+    QZ_LAUNCH(S, st, "k_big_hist", 4 * elems, k_big_hist<TILE><<<grid, kThreads, 0, st>>>(a, bb.key, h4, w0));
+    QZ_LAUNCH(S, st, "k_big_bases", 4ll * kH4 * host_count,
+              k_big_bases<<<grid_cap(4ll * host_count, 1, sms * 8), kThreads, 0, st>>>(a, h4, w0));
     // pass 0: unstable, no look-back (bytes are an upper bound: passes whose
     // digit is constant in a group are skipped for that group)
-    QZ_LAUNCH(S, st, "k_big_pass0", 16 * elems, k_big_pass0<<<grid, kThreads, 0, st>>>(a, h4, bb));
-    // passes 1..3: stable, decoupled look-back; a persistent grid of resident
-    // CTAs (59 KB of shared memory per CTA: three fit an SM), tiles taken by
-    // ticket
-    int pgrid = sms * S->tune.big_ctas_per_sm;
-    for (int pass = 1; pass < 4; ++pass) {
+    QZ_LAUNCH(S, st, "k_big_pass0", 16 * elems, k_big_pass0<TILE><<<grid, kThreads, 0, st>>>(a, h4, bb, w0));
+    // stable passes: decoupled look-back over a persistent grid, tiles taken
+    // by ticket (a tile waits only on tiles of earlier tickets, whose CTAs are
+    // resident, so the grid may exceed what fits at once)
+    const int pgrid = sms * S->tune.big_ctas_per_sm;
+    for (int pass = 1; pass < npass; ++pass) {
         unsigned epoch = ++S->radix_epoch & 0x3fffffffu;
         if (epoch == 0) epoch = ++S->radix_epoch & 0x3fffffffu;
         unsigned* ticket = reinterpret_cast<unsigned*>(cnt + CNT_TICKET);
         cudaMemsetAsync(ticket, 0, sizeof(unsigned), st);
         const bool test = S->tune.lookback_test && pass == 1;
         QZ_LAUNCH(S, st, "k_big_pass", 16 * elems,
-                  k_big_pass<<<pgrid, kThreads, 0, st>>>(a, h4, pass, epoch, bb, f.status64, ticket, S->status,
-                                                         test ? 4096u : kSpinLimit, test ? 1 : -1));
+                  k_big_pass<TILE><<<pgrid, kThreads, 0, st>>>(a, h4, pass, w0, epoch, bb, f.status64, ticket,
+                                                               S->status, test ? 4096u : kSpinLimit,
+                                                               test ? 1 : -1));
+    }
+}
+
+}  // namespace
+
+void sort_big_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
+                     uint32_t* key, int* val, int key_bits, cudaStream_t st) {
+    if (host_count <= 0) return;
+    FwdBuffers& f = S->f;
+    int* cnt = S->counters;
+    const int tile = S->tune.big_tile;
+    big_plan(S, list, d_count, host_count, tile, st);
+    BigArgs a{list, d_count, f.ltbase, f.lwbase, cnt + CNT_LTILES, f.gmask, f.tseg};
+    BigBuffers bb{key, val, {f.wsk[0], f.wsk[1]}, {f.wsv[0], f.wsv[1]}};
+    uint32_t* h4 = f.h4;
+    cudaMemsetAsync(h4, 0, sizeof(uint32_t) * kH4 * (size_t)host_count, st);
+    const int w0 = first_digit_bits(key_bits, S->tune.first_digit_max);
+    const int npass = key_bits <= w0 + 16 ? 3 : 4;  // a fourth pass only when the key needs it
+    switch (tile) {
+        case 2048: big_sort_run<2048>(S, a, bb, h4, host_count, elems, w0, npass, st); break;
+        case 8192: big_sort_run<8192>(S, a, bb, h4, host_count, elems, w0, npass, st); break;
+        default: big_sort_run<4096>(S, a, bb, h4, host_count, elems, w0, npass, st); break;
     }
 }
 

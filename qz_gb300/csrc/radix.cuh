@@ -38,9 +38,12 @@ void sort_rbc_groups(Storage* S, const int2* list, const int* d_count, int host_
 void sort_medium_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
                         const uint32_t* skey, const int* sval, uint32_t* key, int* val, cudaStream_t st);
 // Groups longer than kOT slots, in place in (key, val) (one decoupled
-// look-back pass per digit).
+// look-back pass per digit).  key_bits: the keys are below 2^key_bits, which
+// sets the digit layout (three passes up to 16 + the tuned first-digit width).
 void sort_big_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
-                     uint32_t* key, int* val, cudaStream_t st);
+                     uint32_t* key, int* val, int key_bits, cudaStream_t st);
 size_t tile_sort_smem();
+// Digit-count words per listed group of the large-group sort.
+size_t big_hist_words();
 
 }  // namespace qz

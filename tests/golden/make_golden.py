@@ -27,7 +27,17 @@ sys.path.insert(0, ROOT)
 
 from qz_gb300 import synth  # noqa: E402
 
-REF_BSC = "/root/reference/crates/qz-lib/src/compression/bsc.rs"
+# The reference tree's root comes from the command line (first argument) or
+# the QZ_REFERENCE environment variable; the BSC wrapper sits below it.
+BSC_RS = os.path.join("crates", "qz-lib", "src", "compression", "bsc.rs")
+
+
+def reference_root(argv) -> str:
+    root = argv[1] if len(argv) > 1 else os.environ.get("QZ_REFERENCE", "")
+    if not root or not os.path.exists(os.path.join(root, BSC_RS)):
+        raise SystemExit("usage: make_golden.py <reference tree root>  (or set QZ_REFERENCE); "
+                         f"{BSC_RS} must exist below it")
+    return root
 
 
 def naive(t: bytes, rate: int = 4):
@@ -48,8 +58,8 @@ def naive(t: bytes, rate: int = 4):
     return bytes(out), primary, [aux[k] for k in sorted(aux)]
 
 
-def reference_test_strings() -> list[bytes]:
-    src = open(REF_BSC).read()
+def reference_test_strings(root: str) -> list[bytes]:
+    src = open(os.path.join(root, BSC_RS)).read()
     tests = src[src.index("mod tests"):]
     out = []
     # byte-string literals, joined across Rust's "\<newline><indent>" continuation
@@ -61,7 +71,7 @@ def reference_test_strings() -> list[bytes]:
 
 def main():
     cases = []
-    for i, s in enumerate(reference_test_strings()):
+    for i, s in enumerate(reference_test_strings(reference_root(sys.argv))):
         cases.append((f"bsc_rs_test_{i}", s))
     cases += [
         ("empty", b""),

@@ -8,7 +8,8 @@ from qz_gb300 import autotune
 class FakeStorage:
     def __init__(self):
         self.p = {"fwd_sub_bytes": 64 << 20, "inv_sub_bytes": 64 << 20, "big_ctas_per_sm": 3,
-                  "tile_ctas_per_sm": 3, "medium_max": 512, "ruler_stride_log2": 5}
+                  "tile_ctas_per_sm": 3, "medium_max": 512, "ruler_stride_log2": 5, "big_tile": 4096,
+                  "radix_first_bits": 11}
 
     def set_param(self, k, v):
         self.p[k] = v
@@ -20,7 +21,8 @@ class FakeStorage:
 def test_coordinate_descent_finds_best(tmp_path, monkeypatch):
     monkeypatch.setenv("QZGPU_TUNE_CACHE", str(tmp_path / "tune.json"))
     st = FakeStorage()
-    target = {"fwd_sub_bytes": 32 << 20, "big_ctas_per_sm": 3, "medium_max": 128, "ruler_stride_log2": 6}
+    target = {"fwd_sub_bytes": 32 << 20, "big_ctas_per_sm": 3, "medium_max": 128, "ruler_stride_log2": 6,
+              "big_tile": 8192, "radix_first_bits": 8}
 
     def run():
         # cost falls as each knob approaches its target value

@@ -331,3 +331,24 @@ def test_ultra_block_round_trip(gpu):
         assert np.bincount(u, minlength=256).tolist() == np.bincount(t, minlength=256).tolist()
         (back,) = st.decode_batch([u], [idx])
         assert (back == t).all()
+
+
+@pytest.mark.parametrize("cap,blocks", [(1 << 20, 1), (25 << 20, 4), (200 << 20, 64)])
+def test_storage_bytes_match_allocation(gpu, cap, blocks):
+    # serving admission and qz's VRAM check (check_cuda_vram, bsc.rs:50-82)
+    # rely on qzgpu_storage_bytes predicting what a storage takes from HBM
+    torch = pytest.importorskip("torch")
+    with bwt.Storage(1 << 20, 1) as warm:  # module loading and context set-up happen before measuring
+        warm.encode_batch([np.frombuffer(b"warm-up block", np.uint8)])
+    torch.cuda.synchronize()
+    want = bwt.Storage.device_bytes(cap, blocks)
+    free0, _ = torch.cuda.mem_get_info()
+    st = bwt.Storage(cap, blocks)
+    try:
+        free1, _ = torch.cuda.mem_get_info()
+        taken = free0 - free1
+        lanes = st.get_param("lanes")
+        # each lane is one cudaMalloc, rounded up to the driver's 2 MiB pages
+        assert want <= taken <= want + lanes * (2 << 20) + (4 << 20), (want, taken)
+    finally:
+        st.close()

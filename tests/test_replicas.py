@@ -66,3 +66,22 @@ def test_reference_arm_prints_once_under_torchrun():
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port"
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_cpu_sample_keeps_the_kind_mix_and_rotates_through_every_block():
+    # the chunk's 15 sequence / 13 quality / 5 header blocks, 16 host cores
+    kinds = ["seq"] * 15 + ["qual"] * 13 + ["hdr"] * 5
+    blocks = [bytes([i]) for i in range(len(kinds))]
+    seen = set()
+    for step in range(5):
+        ids, sample, skinds = bench.cpu_sample(blocks, kinds, 16, step=step)
+        assert len(ids) == len(set(ids)) == 16 and ids == sorted(ids)
+        assert [blocks[i] for i in ids] == sample and [kinds[i] for i in ids] == skinds
+        # within one block of the workload's proportions for each kind
+        for k, c in (("seq", 15), ("qual", 13), ("hdr", 5)):
+            assert abs(skinds.count(k) - 16 * c / 33) <= 1.5
+        seen.update(ids)
+    assert seen == set(range(33))
+    # both arms print the same config object for the same workload
+    a = bench.workload_config("w", blocks, 1)
+    assert a == bench.workload_config("w", blocks, 1) and a["blocks"] == 33 and a["bytes"] == 33

@@ -53,3 +53,27 @@ def test_noalloc_rejects_blocks_over_the_limit():
     rc = _noalloc(lib, d.data_ptr(), d.data_ptr(), n, 1, torch.cuda.current_stream().cuda_stream)
     assert rc == native.QZGPU_BLOCK_TOO_LARGE
     assert "larger" in native.error_string(rc)
+
+
+def test_noalloc_in_place_and_large_then_small():
+    # d_T may be d_U (in place), and a small block after a full-size one must
+    # not see the larger call's leftovers in the shared scratch (sizes that are
+    # not multiples of the 4096-byte tiles or the 32-row ruler stride)
+    torch = pytest.importorskip("torch")
+    lib = native.load()
+    bwt.init()
+    stream = torch.cuda.current_stream().cuda_stream
+    g = synth.uniform_genome(80_000, seed=64)
+    blocks = [synth.header_stream(30_000, seed=65)[: native.QZGPU_NOALLOC_MAX_BLOCK],
+              synth.sample_reads(g, 40, seed=66)[:5_997],
+              synth.quality_stream(300, seed=67)[:4_099],
+              np.frombuffer(b"ab", np.uint8).copy()]
+    for t in blocks:
+        u, idx = bwt.bwt_encode(t)
+        expected = bwt.bwt_decode(u, idx)  # existing entry point
+        d = torch.from_numpy(np.ascontiguousarray(u)).cuda()
+        rc = _noalloc(lib, d.data_ptr(), d.data_ptr(), len(u), idx, stream)
+        assert rc == native.QZGPU_NO_ERROR, native.error_string(rc)
+        torch.cuda.synchronize()
+        assert np.array_equal(d.cpu().numpy(), expected)
+        assert np.array_equal(expected, t)
