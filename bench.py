@@ -289,7 +289,8 @@ def one_lane_storage(bwt, nbytes, nblocks, tuned, params):
         else:
             os.environ["QZGPU_LANES"] = old
     for k, v in (tuned or {}).items():
-        st1.set_param(k, int(v))
+        if k in bwt.Storage.PARAMS:  # settable knobs only ("lanes" is read-only)
+            st1.set_param(k, int(v))
     for kv in params:
         k, v = kv.split("=", 1)
         st1.set_param(k, int(v))

@@ -152,6 +152,12 @@ int qzgpu_storage_round_counts(const qzgpu_storage *storage, long long *active, 
  *   "radix_first_bits"                widest first (unstable) radix digit of that sort
  *                                     (8..11): keys of up to 16 + v bits sort in three
  *                                     passes, 8 keeps four passes above 24-bit keys
+ *   "radix_rank"                      how a stable radix pass finds the lanes of a warp that
+ *                                     share a digit: 0 warp match instruction, 1 lane
+ *                                     masks built by shared-memory atomics
+ *   "round_pipeline"                  forward doubling rounds: 0 each round issued after
+ *                                     its counts are read back, 1 issued one round ahead
+ *                                     with launch shapes from bounds
  *   "lookback_test"                   1: failure-detection test (forward calls fail with
  *                                     QZGPU_TIMEOUT through a bounded look-back wait that
  *                                     runs out; no GPU fault); 0: off (default)

@@ -29,6 +29,8 @@ SPACE = {
     "ruler_stride_log2": [4, 5, 6],
     "big_tile": [2048, 4096, 8192],
     "radix_first_bits": [8, 11],
+    "radix_rank": [0, 1],
+    "round_pipeline": [0, 1],
 }
 
 

@@ -18,6 +18,10 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libqzgpu.so")
+# libbsc's BWT-stage symbols over the library (plain C object, linked by a
+# caller together with libqzgpu.so in place of libbsc's own bwt object)
+SHIM_SRC = os.path.join(CSRC, "bsc_bwt_shim.c")
+SHIM_OBJ = os.path.join(OUT, "bsc_bwt_shim.o")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")]
@@ -36,13 +40,14 @@ def sources() -> list[str]:
 
 def _headers() -> list[str]:
     hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    hs.append(os.path.join(ROOT, "include", "qzgpu.h"))
+    inc = os.path.join(ROOT, "include")
+    hs += [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith(".h")]
     return sorted(hs)
 
 
 def _stamp(extra: list[str]) -> str:
     h = hashlib.sha256()
-    for p in sources() + _headers():
+    for p in sources() + _headers() + [SHIM_SRC]:
         with open(p, "rb") as f:
             h.update(p.encode() + f.read())
     h.update(" ".join(NVCC_FLAGS + ARCH + extra).encode())
@@ -54,7 +59,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     os.makedirs(OUT, exist_ok=True)
     stamp_path = os.path.join(OUT, "stamp.txt")
     stamp = _stamp(extra)
-    if not force and os.path.exists(LIB) and os.path.exists(stamp_path):
+    if not force and os.path.exists(LIB) and os.path.exists(SHIM_OBJ) and os.path.exists(stamp_path):
         with open(stamp_path) as f:
             if f.read().strip() == stamp:
                 return LIB
@@ -73,6 +78,11 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
         if verbose and (r.stdout or r.stderr):
             sys.stderr.write(r.stdout + r.stderr)
 
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        raise RuntimeError("a C compiler (gcc) is required to build the libbsc shim object")
+    cmds.append([cc, "-std=c99", "-O2", "-fPIC", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include"), "-c",
+                 SHIM_SRC, "-o", SHIM_OBJ])
     with cf.ThreadPoolExecutor(max_workers=min(8, len(cmds))) as ex:
         list(ex.map(run, cmds))
     tmp = LIB + ".tmp"

@@ -92,6 +92,8 @@ struct Tune {
     int ruler_log2 = 5;        // inverse: a ruler every 2^ruler_log2 rows (3..12)
     int big_tile = 4096;       // slots per look-back tile of the large-group sort (2048, 4096, 8192)
     int first_digit_max = 11;  // widest first radix digit of the large-group sort (8..11 bits)
+    int radix_rank = 0;        // stable radix passes: 0 lanes of a digit by warp match, 1 by shared lane masks
+    int round_pipeline = 0;    // forward rounds: 0 issued after the host reads their counts, 1 issued ahead
     // failure-detection test: in the first stable radix pass the second tile
     // of every group publishes nothing and look-back waits give up after 4096
     // polls, so the tiles after it report QZGPU_TIMEOUT (no GPU fault)
@@ -167,6 +169,11 @@ struct Storage {
     std::vector<long long> rounds_active;  // active suffixes per round of the last forward call
     long long sub_batch_bytes = 64ll << 20;  // forward: blocks grouped up to this size
     unsigned radix_epoch = 0;                // tags look-back status words of each pass
+    cudaEvent_t round_ev[2] = {nullptr, nullptr};  // forward: counters of a split have landed
+    // dry issue: launches are recorded (name, algorithmic bytes) instead of
+    // made, to recompute a pipelined round's bytes from its exact counts
+    bool dry = false;
+    std::vector<std::pair<const char*, long long>> dry_list;
 };
 
 // Lane size of a multi-lane engine (block bytes one lane's sub-batch holds).
@@ -189,7 +196,10 @@ struct Engine {
     bool stop = false;
     bool profile = false;
     std::string profile_only;  // when set, only launches of this kernel are timed
-    long long fwd_sub_bytes = kLaneBytes;  // forward sub-batch size (<= lane_bytes)
+    // forward sub-batch size (<= lane_bytes): 16 MiB keeps a sub-batch's rank
+    // array (64 MB) inside L2 next to the other lanes' random accesses; the
+    // autotuner picked it on the chunk and on 256 uneven blocks
+    long long fwd_sub_bytes = 16ll << 20;
     long long inv_sub_bytes = kLaneBytes;  // inverse sub-batch size (<= lane_bytes)
     qzgpu_stats stats{};
     std::vector<long long> rounds_active;
@@ -258,6 +268,10 @@ void prof_flush(Storage* S);  // after the stream is idle: fold pending records 
 // Launch wrapper: counts the launch, times it when profiling, checks it in debug mode.
 #define QZ_LAUNCH(S, st, name, bytes, ...)                     \
     do {                                                       \
+        if ((S)->dry) {                                        \
+            (S)->dry_list.emplace_back(name, (long long)(bytes)); \
+            break;                                             \
+        }                                                      \
         cudaEvent_t _qz_a = ::qz::prof_begin(S, st, name);     \
         __VA_ARGS__;                                           \
         ::qz::prof_end(S, st, name, (long long)(bytes), _qz_a); \

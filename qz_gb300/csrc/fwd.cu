@@ -1173,7 +1173,6 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
     }
     int cur = 0;
     int act = CNT_ACTIVE;  // counter slot holding the current active count
-    GatherArgs ga{f.R, S->blk_off, nb, S->blk_K, -1};
     // ---- initial sort (groups = blocks)
     // initial keys: up to 32 bits of packed symbols
     sort_groups(S, cnt0, (int)N, S->counters + act, f.key, f.W[0], f.G[0], st, false, 32);
@@ -1236,15 +1235,11 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
     dump_split();
     add_round(S, 0, N);
 
-    int* hcnt = S->pin_rd;
     // rank keys R[x+h] + h + 1 (R < N, h <= n_b) and end keys (<= n_b): below N + max n_b
     int nmax = 0;
     for (int b = 0; b < nb; ++b) nmax = std::max(nmax, n[b]);
     int rank_key_bits = 1;
     while (rank_key_bits < 32 && (1ll << rank_key_bits) <= N + nmax) ++rank_key_bits;
-    int round = 0;
-    long long A_prev = N;
-    int last_mode = kRankNone;
     bool fixed_up = false;
     auto rank_fixup = [&](long long finished) {
         // SA read; one rank written per suffix the initial split finished
@@ -1252,45 +1247,20 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
                   k_rank_fixup<<<grid_for(N, kThreads, S->sms * 16), kThreads, 0, st>>>((int)N, f.SA, f.R));
         fixed_up = true;
     };
-    DevStatus& hst = *reinterpret_cast<DevStatus*>(S->pin_rd + S->cap_blocks + 64);
-    for (;;) {
-        e = cudaMemcpyAsync(hcnt, S->counters, sizeof(int) * CNT_SLOTS, cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(&hst, S->status, sizeof(hst), cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) return map_cuda_error(e);
-        if (hst.error) {
-            // the counters of a round that failed are not to be trusted
-            prof_flush(S);
-            if (debug_on()) debug_log("device status %d at %d detail %lld", hst.error, hst.where, hst.detail);
-            return hst.error;
-        }
-        int A = hcnt[act];
-        // the last split wrote A survivors (8 B) and A_prev - A suffix-array
-        // entries (4 B), and 4 B of rank per slot of round 0's split (none on
-        // the initial split; bounded by the slots on later ones)
-        if (S->profile && !S->prof_pending.empty() && S->prof_pending.back().name &&
-            strncmp(S->prof_pending.back().name, "k_split_apply", 13) == 0)
-            S->prof_pending.back().bytes += 8ll * A + 4ll * (A_prev - A) + (last_mode == kRankAll ? 4ll * A_prev : 0);
-        if (A == 0) break;
-        if (debug_on())
-            debug_log("round %d: active %d rbc %d/%d medium %d/%d tile %d/%d large %d/%d", round, A, hcnt[CNT_PAIR],
-                      hcnt[CNT_PAIR_ELEMS], hcnt[CNT_MED], hcnt[CNT_MED_ELEMS], hcnt[CNT_TILE], hcnt[CNT_TILE_ELEMS],
-                      hcnt[CNT_LARGE], hcnt[CNT_LARGE_ELEMS]);
-        if (round >= kMaxRounds) {
-            if (debug_on()) debug_log("no convergence after %d rounds", round);
-            return QZGPU_GPU_ERROR;
-        }
-        add_round(S, round + 1, A);
-        ga.round = round;
+    GatherArgs ga{f.R, S->blk_off, nb, S->blk_K, 0};
+    // One doubling round on the device.  hc: the round's list counts (exact,
+    // or bounds when the round is issued ahead of its counts); A: its active
+    // slots (or a bound).  Every kernel reads the exact counts from the device.
+    auto issue_round = [&](int r, const int* hc, long long A) {
+        ga.round = r;
         // suffix and group rank read, one rank gathered, key written; small
         // groups inside a warp window sorted on the spot (suffix rewritten)
-        long long small_el = (long long)A - hcnt[CNT_PAIR_ELEMS] - hcnt[CNT_MED_ELEMS] - hcnt[CNT_TILE_ELEMS] -
-                             hcnt[CNT_LARGE_ELEMS];
-        QZ_LAUNCH(S, st, "k_gather_small", 16ll * A + 4ll * small_el,
+        const long long small_el = A - hc[CNT_PAIR_ELEMS] - hc[CNT_MED_ELEMS] - hc[CNT_TILE_ELEMS] -
+                                   hc[CNT_LARGE_ELEMS];
+        QZ_LAUNCH(S, st, "k_gather_small", 16ll * A + 4ll * std::max(small_el, 0ll),
                   k_gather_small<<<grid_for(((A + 31) / 32 + kGatherRun - 1) / kGatherRun, kWarps, S->sms * 16),
-                                   kThreads, 0, st>>>(
-                      S->counters + act, f.G[cur], f.key, f.W[cur], ga, f.straddle));
-        if (round == 0) rank_fixup(N - A);
+                                   kThreads, 0, st>>>(S->counters + act, f.G[cur], f.key, f.W[cur], ga, f.straddle));
+        if (r == 0) rank_fixup(N - A);
         // one flag byte per gather run; flagged runs: group ranks of one window,
         // keys and suffixes of the straddling group
         const long long nruns = ((A + 31) / 32 + kGatherRun - 1) / kGatherRun;
@@ -1298,21 +1268,163 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
                   k_sort_straddle<<<grid_for(nruns, kWarps, S->sms * 16), kThreads, 0, st>>>(
                       S->counters + act, f.G[cur], f.key, f.W[cur], f.straddle));
         // round 0 gathers 32-bit text keys; later rounds rank keys below N + max n_b
-        sort_groups(S, hcnt, A, S->counters + act, f.key, f.W[cur], f.G[cur], st, true,
-                    round == 0 ? 32 : rank_key_bits);
-        if (dump) {
+        sort_groups(S, hc, (int)A, S->counters + act, f.key, f.W[cur], f.G[cur], st, true,
+                    r == 0 ? 32 : rank_key_bits);
+        if (dump && !S->dry) {
             dump_array("rsorted_key", f.key, 4 * (size_t)A, st);
             dump_array("rsorted_W", f.W[cur], 4 * (size_t)A, st);
         }
-        last_mode = round == 0 ? kRankAll : kRankChanged;
-        split(A, last_mode);
-        dump_split();
+        split(A, r == 0 ? kRankAll : kRankChanged);
+        if (!S->dry) dump_split();
+    };
+
+    // ---- doubling rounds.  Host-paced (default): the counters of the split
+    // that lists a round's groups are read back, then the round is issued with
+    // launch shapes from its exact counts.  Pipelined (tune.round_pipeline):
+    // round r is issued before those counters are read, so the device always
+    // has the next round queued; its launch shapes come from bounds (active
+    // counts and group lengths only shrink from round to round, so the
+    // previous round's counts bound this one's) and the round after the last
+    // finds no active slot and returns at once.  It saves the host read's
+    // bubble per round and costs launches sized for bounds plus one empty
+    // round.  Counters and status of each split land in one of two pinned
+    // slots.
+    int* hc[2] = {S->pin_rd, S->pin_rd + CNT_SLOTS};
+    DevStatus* hs[2] = {reinterpret_cast<DevStatus*>(S->pin_rd + S->cap_blocks + 64),
+                        reinterpret_cast<DevStatus*>(S->pin_rd + S->cap_blocks + 68)};
+    auto post = [&](int slot) {
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hc[slot], S->counters, sizeof(int) * CNT_SLOTS, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hs[slot], S->status, sizeof(DevStatus), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaEventRecord(S->round_ev[slot], st);
+    };
+    // largest class with a listed group: a round's groups lie inside the
+    // previous round's, so no later round has a longer one
+    auto top_class = [](const int* h) {
+        return h[CNT_LARGE] ? 4 : h[CNT_TILE] ? 3 : h[CNT_MED] ? 2 : h[CNT_PAIR] ? 1 : 0;
+    };
+    auto bounds = [&](int top, long long A, int* out) {
+        for (int i = 0; i < CNT_SLOTS; ++i) out[i] = 0;
+        const int lo[5] = {0, kSmallMax + 1, 65, S->tune.medium_max + 1, kOT + 1};
+        const int cnt[5] = {0, CNT_PAIR, CNT_MED, CNT_TILE, CNT_LARGE};
+        const int el[5] = {0, CNT_PAIR_ELEMS, CNT_MED_ELEMS, CNT_TILE_ELEMS, CNT_LARGE_ELEMS};
+        for (int c = 1; c <= top; ++c) {
+            out[cnt[c]] = (int)std::max<long long>(1, A / lo[c]);
+            out[el[c]] = (int)A;
+        }
+    };
+    post(0);  // lists of round 0, from the initial split
+    if (e != cudaSuccess) return map_cuda_error(e);
+    int top = top_class(cnt0);  // the initial groups are the blocks
+    long long A_bound = N, A_prev = N;
+    int round = 0;
+    // profile record of the previous round's split apply (its survivors are
+    // known one round later)
+    int last_apply = -1;
+    if (S->profile && !S->prof_pending.empty() && strcmp(S->prof_pending.back().name, "k_split_apply_first") == 0)
+        last_apply = (int)S->prof_pending.size() - 1;
+    int hb[CNT_SLOTS];
+    for (;;) {
+        if (round >= kMaxRounds) {
+            if (debug_on()) debug_log("no convergence after %d rounds", round);
+            cudaStreamSynchronize(st);
+            prof_flush(S);
+            return QZGPU_GPU_ERROR;
+        }
+        const int act_r = act;  // this round's active count lives here
+        const size_t mark = S->prof_pending.size();
+        if (S->tune.round_pipeline) {
+            bounds(top, A_bound, hb);
+            issue_round(round, hb, A_bound);
+            post((round + 1) & 1);
+        }
+        if (e == cudaSuccess) e = cudaEventSynchronize(S->round_ev[round & 1]);
+        if (e != cudaSuccess) return map_cuda_error(e);
+        if (hs[round & 1]->error) {
+            // the counters of a round that failed are not to be trusted
+            const DevStatus ds = *hs[round & 1];
+            cudaStreamSynchronize(st);
+            prof_flush(S);
+            if (debug_on()) debug_log("device status %d at %d detail %lld", ds.error, ds.where, ds.detail);
+            return ds.error;
+        }
+        const int* h = hc[round & 1];
+        const int A = h[act_r];
+        if (!S->tune.round_pipeline) {
+            // host-paced: the round is issued with its exact counts, after they
+            // are read; its launches carry exact bytes
+            if (S->profile && last_apply >= 0)
+                S->prof_pending[last_apply].bytes +=
+                    8ll * A + 4ll * (A_prev - A) + (round == 1 ? 4ll * A_prev : 0);
+            if (A == 0) break;
+            if (debug_on())
+                debug_log("round %d: active %d rbc %d/%d medium %d/%d tile %d/%d large %d/%d", round, A, h[CNT_PAIR],
+                          h[CNT_PAIR_ELEMS], h[CNT_MED], h[CNT_MED_ELEMS], h[CNT_TILE], h[CNT_TILE_ELEMS],
+                          h[CNT_LARGE], h[CNT_LARGE_ELEMS]);
+            add_round(S, round + 1, A);
+            std::copy(h, h + CNT_SLOTS, hb);  // the pinned slot is rewritten by the next post
+            issue_round(round, hb, A);
+            post((round + 1) & 1);
+            last_apply = -1;
+            if (S->profile && !S->prof_pending.empty() && strcmp(S->prof_pending.back().name, "k_split_apply") == 0)
+                last_apply = (int)S->prof_pending.size() - 1;
+            A_prev = A;
+            ++round;
+            continue;
+        }
+        if (S->profile) {
+            // the previous split wrote A survivors (8 B) and A_prev - A
+            // suffix-array entries (4 B), and round 0's split 4 B of rank per slot
+            if (last_apply >= 0)
+                S->prof_pending[last_apply].bytes +=
+                    8ll * A + 4ll * (A_prev - A) + (round == 1 ? 4ll * A_prev : 0);
+            // this round's launches, bytes recomputed from its exact counts
+            // (a launch the exact counts would not make did no work)
+            const bool fu = fixed_up;
+            const int c0 = cur, a0 = act;
+            const unsigned ep = S->radix_epoch;
+            cur = c0 ^ 1;  // the state this round was issued in
+            act = act_r;
+            S->dry = true;
+            S->dry_list.clear();
+            issue_round(round, h, A);
+            S->dry = false;
+            cur = c0;
+            act = a0;
+            fixed_up = fu;
+            S->radix_epoch = ep;
+            // records in issue order (only some kernels may be timed): each
+            // takes the next dry launch of its name
+            size_t k = 0;
+            last_apply = -1;
+            for (size_t i = mark; i < S->prof_pending.size(); ++i) {
+                auto& rec = S->prof_pending[i];
+                size_t j = k;
+                while (j < S->dry_list.size() && strcmp(S->dry_list[j].first, rec.name) != 0) ++j;
+                if (j < S->dry_list.size()) {
+                    rec.bytes = S->dry_list[j].second;
+                    k = j + 1;
+                } else {
+                    rec.bytes = 0;
+                }
+                if (strncmp(rec.name, "k_split_apply", 13) == 0) last_apply = (int)i;
+            }
+        }
+        if (A == 0) break;  // the round just issued finds nothing to do
+        if (debug_on())
+            debug_log("round %d: active %d rbc %d/%d medium %d/%d tile %d/%d large %d/%d", round, A, h[CNT_PAIR],
+                      h[CNT_PAIR_ELEMS], h[CNT_MED], h[CNT_MED_ELEMS], h[CNT_TILE], h[CNT_TILE_ELEMS], h[CNT_LARGE],
+                      h[CNT_LARGE_ELEMS]);
+        add_round(S, round + 1, A);
         A_prev = A;
+        A_bound = A;
+        top = top_class(h);
         ++round;
     }
     if (!fixed_up) rank_fixup(N);  // the initial sort finished every suffix
 
     // ---- U and primary indexes: SA read, one byte gathered, one written
+    int* hcnt = S->pin_rd;
+    DevStatus& hst = *hs[0];
     QZ_LAUNCH(S, st, "k_extract", 6 * N,
               k_extract<<<grid_for(N, kThreads, S->sms * 16), kThreads, 0, st>>>(
                   (int)N, f.SA, f.R, d_T, S->blk_off, nb, d_U, S->blk_idx, aux_rate ? S->blk_aux_rate : nullptr,

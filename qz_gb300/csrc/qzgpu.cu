@@ -67,8 +67,25 @@ cudaEvent_t prof_begin(Storage* S, cudaStream_t st, const char* name) {
     return a;
 }
 
+// Launch log (environment QZGPU_LAUNCH_LOG=<file>): one line per launch,
+// "name algorithmic_bytes", in the order the host issues them, so that a
+// profiler's per-launch counters can be paired with the launches' own bytes.
+static FILE* launch_log() {
+    static FILE* f = [] {
+        const char* p = getenv("QZGPU_LAUNCH_LOG");
+        return (p && *p) ? fopen(p, "w") : nullptr;
+    }();
+    return f;
+}
+
 void prof_end(Storage* S, cudaStream_t st, const char* name, long long bytes, cudaEvent_t a) {
     ++S->launches;
+    if (FILE* f = launch_log()) {
+        static std::mutex mu;
+        std::lock_guard<std::mutex> lk(mu);
+        fprintf(f, "%s %lld\n", name, bytes);
+        fflush(f);
+    }
     if (!a) return;
     cudaEvent_t b = S->ev_pool[S->ev_next++];
     cudaEventRecord(b, st);
@@ -346,6 +363,7 @@ int storage_init(Storage* S, long long cap_bytes, int cap_blocks) {
     S->pin_tab = S->pin;
     S->pin_rd = reinterpret_cast<int*>(S->pin_tab + S->pin_tab_bytes);
     e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&S->round_ev[i], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         storage_free(S);
         return map_cuda_error(e);
@@ -356,6 +374,10 @@ int storage_init(Storage* S, long long cap_bytes, int cap_blocks) {
 void storage_free(Storage* S) {
     for (auto e : S->ev_pool) cudaEventDestroy(e);
     S->ev_pool.clear();
+    for (auto& e : S->round_ev) {
+        if (e) cudaEventDestroy(e);
+        e = nullptr;
+    }
     if (S->stream) cudaStreamDestroy(S->stream);
     if (S->dev) cudaFree(S->dev);
     if (S->pin) cudaFreeHost(S->pin);
@@ -653,6 +675,12 @@ int qzgpu_storage_set_param(qzgpu_storage* storage, const char* name, long long 
     } else if (k == "radix_first_bits") {
         if (value < 8 || value > 11) return QZGPU_BAD_PARAMETER;
         each([&](Tune& t) { t.first_digit_max = (int)value; });
+    } else if (k == "round_pipeline") {
+        if (value < 0 || value > 1) return QZGPU_BAD_PARAMETER;
+        each([&](Tune& t) { t.round_pipeline = (int)value; });
+    } else if (k == "radix_rank") {
+        if (value < 0 || value > 1) return QZGPU_BAD_PARAMETER;
+        each([&](Tune& t) { t.radix_rank = (int)value; });
     } else if (k == "lookback_test") {
         if (value < 0 || value > 1) return QZGPU_BAD_PARAMETER;
         each([&](Tune& t) { t.lookback_test = (int)value; });
@@ -674,6 +702,8 @@ long long qzgpu_storage_get_param(const qzgpu_storage* storage, const char* name
     if (k == "ruler_stride_log2") return t.ruler_log2;
     if (k == "big_tile") return t.big_tile;
     if (k == "radix_first_bits") return t.first_digit_max;
+    if (k == "radix_rank") return t.radix_rank;
+    if (k == "round_pipeline") return t.round_pipeline;
     if (k == "lookback_test") return t.lookback_test;
     if (k == "lanes") return (long long)storage->lanes.size();
     return QZGPU_BAD_PARAMETER;

@@ -300,6 +300,13 @@ __global__ void __launch_bounds__(kThreads) k_big_hist(BigArgs a, const uint32_t
     }
 }
 
+// Zeroes the digit counts of the listed groups (their number read on the device).
+__global__ void __launch_bounds__(kThreads) k_big_clear(uint4* __restrict__ h4, const int* __restrict__ d_count) {
+    const long long n = (long long)*d_count * (kH4 / 4);
+    for (long long i = blockIdx.x * (long long)kThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kThreads)
+        h4[i] = make_uint4(0, 0, 0, 0);
+}
+
 // Per group and pass: exclusive prefix over the pass's digits (in place), and
 // the pass is marked needed unless one digit holds the whole group.
 __global__ void __launch_bounds__(kThreads) k_big_bases(BigArgs a, uint32_t* __restrict__ h4, int w0) {
@@ -470,24 +477,27 @@ __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass0(Bi
 template <int TILE>
 __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass(
     BigArgs a, const uint32_t* __restrict__ h4, int pass, int w0, unsigned epoch, BigBuffers bb,
-    unsigned long long* status, unsigned* ticket, DevStatus* st, unsigned spin_limit, int silent_tile) {
+    unsigned long long* status, unsigned* ticket, DevStatus* st, unsigned spin_limit, int silent_tile,
+    bool atomic_peers) {
     constexpr int IT = TILE / kThreads, WSPAN = TILE / kWarps;
     __shared__ uint32_t skey[TILE];
     __shared__ int sval[TILE];
     __shared__ int vst[TILE];  // the tile's values in slot order (asynchronous copies)
     __shared__ uint32_t wcnt[kWarps][256];
+    __shared__ uint32_t wmask[kWarps][256];  // lane masks per digit (atomic_peers ranking)
     __shared__ uint32_t dig_off[256];
     __shared__ uint32_t gbase[256];
     __shared__ uint32_t sh[kWarps + 1];
     __shared__ int s_tau, s_seg;
     const unsigned w = warp_id(), ln = lane_id();
-    const unsigned lt_mask = (1u << ln) - 1u;
     const int shift = digit_shift(pass, w0);
     const unsigned long long ep = (unsigned long long)epoch << 34;
     // an earlier pass that failed leaves keys whose digits no longer match the
     // group histograms, so the positions below would not stay in the group
     if (failed(st)) return;
     const int TT = *a.ntiles;
+#pragma unroll
+    for (int q = 0; q < kWarps; ++q) wmask[q][threadIdx.x] = 0;  // left zero by every ranking step
     for (;;) {
         if (threadIdx.x == 0) {
             s_tau = (int)atomicAdd(ticket, 1u);
@@ -528,15 +538,8 @@ __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass(
         for (int it = 0; it < IT; ++it) {
             int i = (int)w * WSPAN + it * 32 + (int)ln;
             bool valid = i < cnt;
-            uint32_t kv = kr[it];
-            unsigned dg = valid ? (kv >> shift) & 255u : 256u;
-            unsigned peers = __match_any_sync(0xffffffffu, dg);
-            unsigned before = __popc(peers & lt_mask);
-            uint32_t prev = valid ? wcnt[w][dg] : 0u;
-            __syncwarp();
-            if (valid && before == 0) wcnt[w][dg] = prev + __popc(peers);
-            __syncwarp();
-            rk[it] = prev + before;
+            unsigned dg = (kr[it] >> shift) & 255u;
+            rk[it] = warp_digit_rank(dg, valid, wcnt[w], wmask[w], atomic_peers);
         }
         __syncthreads();
         {
@@ -680,12 +683,12 @@ void big_sort_run(Storage* S, const BigArgs& a, const BigBuffers& bb, uint32_t* 
         unsigned epoch = ++S->radix_epoch & 0x3fffffffu;
         if (epoch == 0) epoch = ++S->radix_epoch & 0x3fffffffu;
         unsigned* ticket = reinterpret_cast<unsigned*>(cnt + CNT_TICKET);
-        cudaMemsetAsync(ticket, 0, sizeof(unsigned), st);
+        if (!S->dry) cudaMemsetAsync(ticket, 0, sizeof(unsigned), st);
         const bool test = S->tune.lookback_test && pass == 1;
         QZ_LAUNCH(S, st, "k_big_pass", 16 * elems,
                   k_big_pass<TILE><<<pgrid, kThreads, 0, st>>>(a, h4, pass, w0, epoch, bb, f.status64, ticket,
                                                                S->status, test ? 4096u : kSpinLimit,
-                                                               test ? 1 : -1));
+                                                               test ? 1 : -1, S->tune.radix_rank != 0));
     }
 }
 
@@ -701,7 +704,10 @@ void sort_big_groups(Storage* S, const int2* list, const int* d_count, int host_
     BigArgs a{list, d_count, f.ltbase, f.lwbase, cnt + CNT_LTILES, f.gmask, f.tseg};
     BigBuffers bb{key, val, {f.wsk[0], f.wsk[1]}, {f.wsv[0], f.wsv[1]}};
     uint32_t* h4 = f.h4;
-    cudaMemsetAsync(h4, 0, sizeof(uint32_t) * kH4 * (size_t)host_count, st);
+    // digit counts of the listed groups cleared (host_count may be a bound)
+    QZ_LAUNCH(S, st, "k_big_clear", 4ll * kH4 * host_count,
+              k_big_clear<<<grid_cap(host_count * (long long)(kH4 / 4), kThreads, S->sms * 4), kThreads, 0, st>>>(
+                  reinterpret_cast<uint4*>(h4), d_count));
     const int w0 = first_digit_bits(key_bits, S->tune.first_digit_max);
     const int npass = key_bits <= w0 + 16 ? 3 : 4;  // a fourth pass only when the key needs it
     switch (tile) {

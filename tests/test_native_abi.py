@@ -109,3 +109,50 @@ def test_c_program_compiles_and_links(lib, tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
 
+
+
+SHIM_CALLER = r"""
+/* A libbsc-side caller: it knows only libbsc's BWT-stage names and links
+ * against the shim object plus the library, as libbsc would once its own bwt
+ * object is left out.  With a block as argument it sorts it and prints the
+ * transform and primary index, then inverts it in place. */
+#include <stdio.h>
+#include <string.h>
+#include "qzgpu_bsc_shim.h"
+
+int main(int argc, char **argv) {
+    if (argc < 2) return 0; /* linked, not run: no GPU needed */
+    unsigned char t[4096];
+    int n = (int)strlen(argv[1]);
+    if (n > 4096) return 2;
+    memcpy(t, argv[1], (size_t)n);
+    int idx = bsc_bwt_encode(t, n, NULL, NULL, 1);
+    if (idx < 0) return 3;
+    printf("%.*s %d\n", n, (const char *)t, idx);
+    if (bsc_bwt_decode(t, n, idx, 0, NULL, 1) != 0) return 4;
+    printf("%.*s\n", n, (const char *)t);
+    return 0;
+}
+"""
+
+
+def build_shim_caller(tmp_path):
+    build.build()
+    src = tmp_path / "bsc_caller.c"
+    src.write_text(SHIM_CALLER)
+    exe = tmp_path / "bsc_caller"
+    libdir = os.path.dirname(native.LIB_PATH)
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-pedantic", "-I", os.path.join(ROOT, "include"),
+                        str(src), build.SHIM_OBJ, "-o", str(exe), "-L", libdir, "-lqzgpu", f"-Wl,-rpath,{libdir}"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_bsc_shim_exports_libbsc_names_and_links(lib, tmp_path):
+    out = subprocess.run(["nm", "--defined-only", build.SHIM_OBJ], capture_output=True, text=True,
+                         check=True).stdout
+    assert set(re.findall(r"\sT\s+(\w+)", out)) == {"bsc_bwt_encode", "bsc_bwt_decode"}
+    exe = build_shim_caller(tmp_path)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
