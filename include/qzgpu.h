@@ -143,7 +143,7 @@ int qzgpu_storage_round_counts(const qzgpu_storage *storage, long long *active, 
 
 /* Runtime tuning of a storage (set by the autotuner, qz_gb300/autotune.py):
  *   "fwd_sub_bytes", "inv_sub_bytes"  block bytes per sub-batch taken by a lane
- *   "big_ctas_per_sm"                 persistent CTAs per SM of a radix pass (1..3)
+ *   "big_ctas_per_sm"                 persistent CTAs per SM of a radix pass (1..4)
  *   "tile_ctas_per_sm"                CTAs per SM of the one-CTA group sort (1..3)
  *   "medium_max"                      longest group sorted by one warp (64..512)
  *   "ruler_stride_log2"               inverse: a ruler every 2^v rows (3..12)
@@ -152,9 +152,6 @@ int qzgpu_storage_round_counts(const qzgpu_storage *storage, long long *active, 
  *   "radix_first_bits"                widest first (unstable) radix digit of that sort
  *                                     (8..11): keys of up to 16 + v bits sort in three
  *                                     passes, 8 keeps four passes above 24-bit keys
- *   "radix_rank"                      how a stable radix pass finds the lanes of a warp that
- *                                     share a digit: 0 warp match instruction, 1 lane
- *                                     masks built by shared-memory atomics
  *   "round_pipeline"                  forward doubling rounds: 0 each round issued after
  *                                     its counts are read back, 1 issued one round ahead
  *                                     with launch shapes from bounds

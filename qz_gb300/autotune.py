@@ -23,13 +23,12 @@ import numpy as np
 SPACE = {
     "fwd_sub_bytes": [16 << 20, 32 << 20, 64 << 20],
     "inv_sub_bytes": [16 << 20, 32 << 20, 64 << 20],
-    "big_ctas_per_sm": [2, 3],
+    "big_ctas_per_sm": [2, 3, 4],
     "tile_ctas_per_sm": [1, 2, 3],
     "medium_max": [64, 128, 256, 512],
     "ruler_stride_log2": [4, 5, 6],
     "big_tile": [2048, 4096, 8192],
     "radix_first_bits": [8, 11],
-    "radix_rank": [0, 1],
     "round_pipeline": [0, 1],
 }
 

@@ -84,29 +84,14 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // same digit, plus the running count of that digit (per-warp counters `cnt`,
 // one per digit): returns the count before this warp step plus the lanes with
 // the same digit below this one, and advances the count.  The lanes with the
-// same digit come either from the warp match instruction (atomic_peers ==
-// false), whose cost grows with the number of distinct digits in the warp,
-// or from a per-digit lane mask in shared memory that each lane ORs its bit
-// into (`mask`: zero on entry, left zero).  Invalid lanes take no part.
-__device__ __forceinline__ uint32_t warp_digit_rank(unsigned dg, bool valid, uint32_t* cnt, uint32_t* mask,
-                                                    bool atomic_peers) {
-    const unsigned ln = lane_id();
-    const unsigned lt = (1u << ln) - 1u;
-    unsigned peers;
-    if (atomic_peers) {
-        if (valid) atomicOr(mask + dg, 1u << ln);
-        __syncwarp();
-        peers = valid ? mask[dg] : 0u;
-    } else {
-        peers = __match_any_sync(0xffffffffu, valid ? dg : 0x10000u);
-    }
+// same digit come from the warp match instruction; invalid lanes take no part.
+__device__ __forceinline__ uint32_t warp_digit_rank(unsigned dg, bool valid, uint32_t* cnt) {
+    const unsigned lt = (1u << lane_id()) - 1u;
+    const unsigned peers = __match_any_sync(0xffffffffu, valid ? dg : 0x10000u);
     const unsigned before = __popc(peers & lt);
     const uint32_t prev = valid ? cnt[dg] : 0u;
     __syncwarp();
-    if (valid && before == 0) {
-        cnt[dg] = prev + __popc(peers);
-        if (atomic_peers) mask[dg] = 0u;
-    }
+    if (valid && before == 0) cnt[dg] = prev + __popc(peers);
     __syncwarp();
     return prev + before;
 }

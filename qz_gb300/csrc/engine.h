@@ -64,6 +64,8 @@ struct FwdBuffers {
     uint32_t* ltbase;
     uint32_t* lwbase;
     uint32_t* tseg;    // large: group of each look-back tile
+    int4* tdesc;       // large: per look-back tile, its group's descriptor (written by pass 0)
+    int2* tdesc2;
     uint32_t* p_surv;  // split: per 256-slot warp tile
     int* p_sub;
     int* p_grp;
@@ -86,13 +88,12 @@ struct InvBuffers {
 
 // Runtime tuning knobs of a lane (set through qzgpu_storage_set_param).
 struct Tune {
-    int big_ctas_per_sm = 3;   // persistent CTAs of a look-back radix pass (59 KB of shared memory each)
+    int big_ctas_per_sm = 3;   // persistent CTAs per SM of a look-back radix pass (1..4)
     int tile_ctas_per_sm = 3;  // CTAs of the one-CTA group sort
     int medium_max = kMedMax;  // longest group sorted by one warp (64..512)
     int ruler_log2 = 5;        // inverse: a ruler every 2^ruler_log2 rows (3..12)
     int big_tile = 4096;       // slots per look-back tile of the large-group sort (2048, 4096, 8192)
     int first_digit_max = 11;  // widest first radix digit of the large-group sort (8..11 bits)
-    int radix_rank = 0;        // stable radix passes: 0 lanes of a digit by warp match, 1 by shared lane masks
     int round_pipeline = 0;    // forward rounds: 0 issued after the host reads their counts, 1 issued ahead
     // failure-detection test: in the first stable radix pass the second tile
     // of every group publishes nothing and look-back waits give up after 4096

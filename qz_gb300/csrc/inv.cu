@@ -318,32 +318,42 @@ __device__ __forceinline__ int ruler_start(const InvArgs& a, const RulerArgs& r,
     return (n + 1) - D;
 }
 
-// Staged bytes to their places: one warp per ruler, lane t takes byte t (its
-// run is contiguous, so a warp's stores are).
+// Staged bytes to their places.  A warp takes 32 consecutive rulers: lane l
+// loads ruler l's length and distance (coalesced), then the warp copies the
+// rulers' runs one after the other, lane t taking byte t (a run is contiguous,
+// so a warp's stores are).
 __global__ void __launch_bounds__(kThreads) k_inv_place(InvArgs a, RulerArgs r, int nb, int Mtot,
                                                         uint8_t* __restrict__ T) {
     const int ln = (int)lane_id();
     const int nwarps = gridDim.x * kWarps;
-    for (int q = blockIdx.x * kWarps + (int)warp_id(); q < Mtot; q += nwarps) {
-        const int b = block_of(a.rbase, nb, q);
-        const int bs = __ldg(a.off + b), n = __ldg(a.off + b + 1) - bs;
-        const int lq = q - __ldg(a.rbase + b);
-        const int L = r.len[q];
-        const int d0 = ruler_start(a, r, b, n, lq, q);
-        if (d0 < 0) {
-            if (ln == 0) report_block(a.st, a.bst, QZGPU_DATA_CORRUPT, 11, b);
-            continue;
+    for (int q0 = (blockIdx.x * kWarps + (int)warp_id()) * 32; q0 < Mtot; q0 += nwarps * 32) {
+        const int q = q0 + ln;
+        int L = 0, d0 = -1, bs = 0, n = 0, b = 0;
+        if (q < Mtot) {
+            b = block_of(a.rbase, nb, q);
+            bs = __ldg(a.off + b);
+            n = __ldg(a.off + b + 1) - bs;
+            L = r.len[q];
+            d0 = ruler_start(a, r, b, n, q - __ldg(a.rbase + b), q);
+            if (d0 < 0) report_block(a.st, a.bst, QZGPU_DATA_CORRUPT, 11, b);
         }
-        const int m = min(L, r.cap);
-        const uint8_t* src = r.stage + (size_t)q * r.cap;
-        for (int t = ln; t < m; t += 32) {
-            const int s = n - d0 - t;
-            if (s >= n) continue;  // row 0: the sentinel, no output byte
-            if (s < 0) {
-                report_block(a.st, a.bst, QZGPU_DATA_CORRUPT, 13, b);
-                break;
+        const int last = min(32, Mtot - q0);
+        for (int k = 0; k < last; ++k) {
+            const int Lk = __shfl_sync(0xffffffffu, L, k), dk = __shfl_sync(0xffffffffu, d0, k);
+            const int bsk = __shfl_sync(0xffffffffu, bs, k), nk = __shfl_sync(0xffffffffu, n, k);
+            const int bk = __shfl_sync(0xffffffffu, b, k);
+            if (dk < 0) continue;  // uniform across the warp
+            const int m = min(Lk, r.cap);
+            const uint8_t* src = r.stage + (size_t)(q0 + k) * r.cap;
+            for (int t = ln; t < m; t += 32) {
+                const int s = nk - dk - t;
+                if (s >= nk) continue;  // row 0: the sentinel, no output byte
+                if (s < 0) {
+                    report_block(a.st, a.bst, QZGPU_DATA_CORRUPT, 13, bk);
+                    break;
+                }
+                T[bsk + s] = src[t];
             }
-            T[bs + s] = src[t];
         }
     }
 }
@@ -554,7 +564,7 @@ int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t*
     // heads again: ruler list read, every ruler's distance written
     QZ_LAUNCH(S, st, "k_inv_spread", 12ll * Mtot, k_inv_spread<<<nrt, kThreads, 0, st>>>(a, r, v.hdist[cur]));
     // staged bytes read and written once
-    const int pgrid = (int)std::min<long long>(((long long)Mtot + kWarps - 1) / kWarps, (long long)S->sms * 16);
+    const int pgrid = (int)std::min<long long>(((long long)Mtot + 32 * kWarps - 1) / (32 * kWarps), (long long)S->sms * 16);
     QZ_LAUNCH(S, st, "k_inv_place", 2 * N + 12ll * Mtot,
               k_inv_place<<<pgrid, kThreads, 0, st>>>(a, r, nb, Mtot, d_T));
     // walks longer than the staging slot: their tails only

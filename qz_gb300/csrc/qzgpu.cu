@@ -220,6 +220,8 @@ size_t layout(Storage* S, char* base, const Caps& c) {
     f.ltbase = cv.take<uint32_t>(c.large + 1);
     f.lwbase = cv.take<uint32_t>(c.large + 1);
     f.tseg = cv.take<uint32_t>(c.big_tiles);
+    f.tdesc = cv.take<int4>(c.big_tiles);
+    f.tdesc2 = cv.take<int2>(c.big_tiles);
     size_t wt = c.N / 256 + 2;
     f.p_surv = cv.take<uint32_t>(wt);
     f.p_sub = cv.take<int>(wt);
@@ -658,7 +660,9 @@ int qzgpu_storage_set_param(qzgpu_storage* storage, const char* name, long long 
         if (value < (1 << 20)) return QZGPU_BAD_PARAMETER;
         (k[0] == 'f' ? storage->fwd_sub_bytes : storage->inv_sub_bytes) = value;
     } else if (k == "big_ctas_per_sm") {
-        if (value < 1 || value > 3) return QZGPU_BAD_PARAMETER;  // all CTAs must stay resident
+        // a tile waits only on tiles of earlier tickets, which resident CTAs
+        // hold, so CTAs beyond residency only queue
+        if (value < 1 || value > 4) return QZGPU_BAD_PARAMETER;
         each([&](Tune& t) { t.big_ctas_per_sm = (int)value; });
     } else if (k == "tile_ctas_per_sm") {
         if (value < 1 || value > 3) return QZGPU_BAD_PARAMETER;
@@ -678,9 +682,6 @@ int qzgpu_storage_set_param(qzgpu_storage* storage, const char* name, long long 
     } else if (k == "round_pipeline") {
         if (value < 0 || value > 1) return QZGPU_BAD_PARAMETER;
         each([&](Tune& t) { t.round_pipeline = (int)value; });
-    } else if (k == "radix_rank") {
-        if (value < 0 || value > 1) return QZGPU_BAD_PARAMETER;
-        each([&](Tune& t) { t.radix_rank = (int)value; });
     } else if (k == "lookback_test") {
         if (value < 0 || value > 1) return QZGPU_BAD_PARAMETER;
         each([&](Tune& t) { t.lookback_test = (int)value; });
@@ -702,7 +703,6 @@ long long qzgpu_storage_get_param(const qzgpu_storage* storage, const char* name
     if (k == "ruler_stride_log2") return t.ruler_log2;
     if (k == "big_tile") return t.big_tile;
     if (k == "radix_first_bits") return t.first_digit_max;
-    if (k == "radix_rank") return t.radix_rank;
     if (k == "round_pipeline") return t.round_pipeline;
     if (k == "lookback_test") return t.lookback_test;
     if (k == "lanes") return (long long)storage->lanes.size();

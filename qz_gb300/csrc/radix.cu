@@ -371,8 +371,10 @@ __device__ __forceinline__ BigRoute big_route(const BigBuffers& bb, const int2 d
     return r;
 }
 
+// Resident CTAs per SM each tile size is compiled for (registers per thread
+// follow): 8192-slot tiles fit two by shared memory, 2048-slot tiles four.
 template <int TILE>
-constexpr int big_min_ctas() { return TILE >= 8192 ? 2 : 3; }
+constexpr int big_min_ctas() { return TILE >= 8192 ? 2 : (TILE <= 2048 ? 4 : 3); }
 
 // Pass 0 (the low w0 bits).  Equal keys may leave a group sort in any order
 // (the split gives them one rank), so this pass needs no stability: a tile
@@ -400,13 +402,18 @@ __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass0(Bi
         __syncthreads();
         const int s = s_seg;
         const uint32_t m = big_passes(a.gmask[s]);
+        const int2 d = a.list[s];
+        const int j = tau - (int)a.tbase[s];
+        const uint32_t wb = a.wbase[s];
+        // the stable passes find everything about this tile in one place
+        if (threadIdx.x == 0) {
+            a.tdesc[tau] = make_int4(s, (int)m, d.x, (int)wb);
+            a.tdesc2[tau] = make_int2(j, d.y);
+        }
         if (!(m & 1u)) {
             __syncthreads();
             continue;  // uniform across the CTA
         }
-        const int2 d = a.list[s];
-        const int j = tau - (int)a.tbase[s];
-        const uint32_t wb = a.wbase[s];
         const BigRoute rt = big_route(bb, d, wb, m, 0);
         const uint32_t* sk = rt.sk;
         const int* sv = rt.sv;
@@ -477,18 +484,18 @@ __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass0(Bi
 template <int TILE>
 __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass(
     BigArgs a, const uint32_t* __restrict__ h4, int pass, int w0, unsigned epoch, BigBuffers bb,
-    unsigned long long* status, unsigned* ticket, DevStatus* st, unsigned spin_limit, int silent_tile,
-    bool atomic_peers) {
+    unsigned long long* status, unsigned* ticket, DevStatus* st, unsigned spin_limit, int silent_tile) {
     constexpr int IT = TILE / kThreads, WSPAN = TILE / kWarps;
     __shared__ uint32_t skey[TILE];
     __shared__ int sval[TILE];
     __shared__ int vst[TILE];  // the tile's values in slot order (asynchronous copies)
     __shared__ uint32_t wcnt[kWarps][256];
-    __shared__ uint32_t wmask[kWarps][256];  // lane masks per digit (atomic_peers ranking)
     __shared__ uint32_t dig_off[256];
     __shared__ uint32_t gbase[256];
     __shared__ uint32_t sh[kWarps + 1];
-    __shared__ int s_tau, s_seg;
+    __shared__ int s_tau;
+    __shared__ int4 s_d;
+    __shared__ int2 s_d2;
     const unsigned w = warp_id(), ln = lane_id();
     const int shift = digit_shift(pass, w0);
     const unsigned long long ep = (unsigned long long)epoch << 34;
@@ -496,29 +503,31 @@ __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass(
     // group histograms, so the positions below would not stay in the group
     if (failed(st)) return;
     const int TT = *a.ntiles;
-#pragma unroll
-    for (int q = 0; q < kWarps; ++q) wmask[q][threadIdx.x] = 0;  // left zero by every ranking step
     for (;;) {
         if (threadIdx.x == 0) {
+            // the ticket, then the tile's descriptor in one dependent load
             s_tau = (int)atomicAdd(ticket, 1u);
-            s_seg = s_tau < TT ? (int)a.tseg[s_tau] : 0;
+            if (s_tau < TT) {
+                s_d = a.tdesc[s_tau];
+                s_d2 = a.tdesc2[s_tau];
+            }
         }
 #pragma unroll
         for (int q = 0; q < kWarps; ++q) wcnt[q][threadIdx.x] = 0;
         __syncthreads();
         int tau = s_tau;
         if (tau >= TT) return;
-        int s = s_seg;
-        const uint32_t m = big_passes(a.gmask[s]);
+        const int s = s_d.x;
+        const uint32_t m = (uint32_t)s_d.y;
         if (!(m >> pass & 1u)) {
             // nothing to sort on this digit: the group's slots stay put and no
             // tile of it looks back at this one
             __syncthreads();
             continue;
         }
-        int2 d = a.list[s];
-        int j = tau - (int)a.tbase[s];
-        const BigRoute rt = big_route(bb, d, a.wbase[s], m, pass);
+        const int2 d = make_int2(s_d.z, s_d2.y);
+        const int j = s_d2.x;
+        const BigRoute rt = big_route(bb, d, (uint32_t)s_d.w, m, pass);
         const uint32_t* srck = rt.sk;
         const int* srcv = rt.sv;
         uint32_t* dstk = rt.dk;
@@ -534,12 +543,15 @@ __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass(
             kr[it] = i < cnt ? __ldg(srck + srcbase + i) : 0u;
             if (i < cnt) cp_async4(vst + i, srcv + srcbase + i);
         }
+        // this thread's digit: the group's base for it, fetched while the keys
+        // are in flight and kept in shared memory until the look-back ends
+        gbase[threadIdx.x] = h4[(size_t)s * kH4 + h4_row(pass) + threadIdx.x];
 #pragma unroll
         for (int it = 0; it < IT; ++it) {
             int i = (int)w * WSPAN + it * 32 + (int)ln;
             bool valid = i < cnt;
             unsigned dg = (kr[it] >> shift) & 255u;
-            rk[it] = warp_digit_rank(dg, valid, wcnt[w], wmask[w], atomic_peers);
+            rk[it] = warp_digit_rank(dg, valid, wcnt[w]);
         }
         __syncthreads();
         {
@@ -582,7 +594,7 @@ __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass(
             }
             uint32_t tot;
             dig_off[dg] = block_excl_sum(run, sh, &tot);
-            gbase[dg] = h4[(size_t)s * kH4 + h4_row(pass) + dg] + excl;
+            gbase[dg] += excl;
         }
         cp_async_wait_all();  // each thread reads back only the values it copied
         __syncthreads();
@@ -688,7 +700,7 @@ void big_sort_run(Storage* S, const BigArgs& a, const BigBuffers& bb, uint32_t* 
         QZ_LAUNCH(S, st, "k_big_pass", 16 * elems,
                   k_big_pass<TILE><<<pgrid, kThreads, 0, st>>>(a, h4, pass, w0, epoch, bb, f.status64, ticket,
                                                                S->status, test ? 4096u : kSpinLimit,
-                                                               test ? 1 : -1, S->tune.radix_rank != 0));
+                                                               test ? 1 : -1));
     }
 }
 
@@ -701,7 +713,7 @@ void sort_big_groups(Storage* S, const int2* list, const int* d_count, int host_
     int* cnt = S->counters;
     const int tile = S->tune.big_tile;
     big_plan(S, list, d_count, host_count, tile, st);
-    BigArgs a{list, d_count, f.ltbase, f.lwbase, cnt + CNT_LTILES, f.gmask, f.tseg};
+    BigArgs a{list, d_count, f.ltbase, f.lwbase, cnt + CNT_LTILES, f.gmask, f.tseg, f.tdesc, f.tdesc2};
     BigBuffers bb{key, val, {f.wsk[0], f.wsk[1]}, {f.wsv[0], f.wsv[1]}};
     uint32_t* h4 = f.h4;
     // digit counts of the listed groups cleared (host_count may be a bound)

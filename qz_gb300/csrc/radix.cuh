@@ -12,6 +12,8 @@ struct BigArgs {
     const int* ntiles;       // total tiles (device)
     uint32_t* gmask;         // per group: passes whose digit is not constant (bit p)
     uint32_t* tseg;          // group of each tile (written by the histogram kernel)
+    int4* tdesc;             // per tile, written by pass 0 for the stable passes:
+    int2* tdesc2;            //   (group, pass mask, first slot, workspace base), (tile in group, length)
 };
 
 // Where a group's slots are before / after one of its needed passes: the first

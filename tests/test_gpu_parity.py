@@ -175,11 +175,11 @@ def test_lookback_wait_runs_out_without_fault(gpu, oracle):
 
 @pytest.mark.parametrize("params", [
     {"medium_max": 64, "big_ctas_per_sm": 2, "ruler_stride_log2": 3, "round_pipeline": 1},
-    {"medium_max": 512, "big_ctas_per_sm": 3, "fwd_sub_bytes": 1 << 20, "big_tile": 2048, "radix_rank": 1},
+    {"medium_max": 512, "big_ctas_per_sm": 4, "fwd_sub_bytes": 1 << 20, "big_tile": 2048},
     {"medium_max": 128, "tile_ctas_per_sm": 1, "ruler_stride_log2": 7, "fwd_sub_bytes": 1 << 20,
      "inv_sub_bytes": 1 << 20, "big_tile": 8192, "radix_first_bits": 8, "round_pipeline": 1},
     {"medium_max": 256, "big_ctas_per_sm": 1, "ruler_stride_log2": 4, "radix_first_bits": 9},
-    {"ruler_stride_log2": 12, "round_pipeline": 1, "radix_rank": 1},
+    {"ruler_stride_log2": 12, "round_pipeline": 1, "big_ctas_per_sm": 4},
 ])
 def test_tuned_knobs_keep_results(gpu, oracle, params):
     rng = np.random.default_rng(99)
