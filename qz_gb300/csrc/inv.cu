@@ -83,7 +83,6 @@ __global__ void __launch_bounds__(kThreads) k_inv_down(InvArgs a, const uint32_t
     __shared__ uint32_t wcnt[kWarps][256];
     __shared__ uint32_t base_of[256];
     const unsigned w = warp_id(), ln = lane_id();
-    const unsigned lt_mask = (1u << ln) - 1u;
     int2 tl = a.tiles[blockIdx.x];
     int b = tl.x, s0 = tl.y;
     int bs = a.off[b], n = a.off[b + 1] - bs;
@@ -98,25 +97,28 @@ __global__ void __launch_bounds__(kThreads) k_inv_down(InvArgs a, const uint32_t
     uint8_t cc[kIRItems];
     uint32_t rk[kIRItems];
     unsigned cu[kIRItems];
-    // all of the tile's symbols in flight at once, then the ranking
+    // all of the tile's symbols in flight at once, then the ranking; full
+    // tiles without per-slot predicates
+    if (cnt == kInitTile) {
 #pragma unroll
-    for (int it = 0; it < kIRItems; ++it) {
-        int i = (int)w * kIRWarpSpan + it * 32 + (int)ln;
-        cu[it] = i < cnt ? (unsigned)__ldg(a.U + s0 + i) : 256u;
-    }
+        for (int it = 0; it < kIRItems; ++it) cu[it] = (unsigned)__ldg(a.U + s0 + (int)w * kIRWarpSpan + it * 32 + (int)ln);
 #pragma unroll
-    for (int it = 0; it < kIRItems; ++it) {
-        int i = (int)w * kIRWarpSpan + it * 32 + (int)ln;
-        bool valid = i < cnt;
-        unsigned c = cu[it];
-        unsigned peers = __match_any_sync(0xffffffffu, c);
-        unsigned before = __popc(peers & lt_mask);
-        uint32_t prev = valid ? wcnt[w][c] : 0u;
-        __syncwarp();
-        if (valid && before == 0) wcnt[w][c] = prev + __popc(peers);
-        __syncwarp();
-        cc[it] = (uint8_t)c;
-        rk[it] = prev + before;
+        for (int it = 0; it < kIRItems; ++it) {
+            cc[it] = (uint8_t)cu[it];
+            rk[it] = warp_digit_rank(cu[it], true, wcnt[w]);
+        }
+    } else {
+#pragma unroll
+        for (int it = 0; it < kIRItems; ++it) {
+            int i = (int)w * kIRWarpSpan + it * 32 + (int)ln;
+            cu[it] = i < cnt ? (unsigned)__ldg(a.U + s0 + i) : 0u;
+        }
+#pragma unroll
+        for (int it = 0; it < kIRItems; ++it) {
+            int i = (int)w * kIRWarpSpan + it * 32 + (int)ln;
+            cc[it] = (uint8_t)cu[it];
+            rk[it] = warp_digit_rank(cu[it], i < cnt, wcnt[w]);
+        }
     }
     __syncthreads();
     {

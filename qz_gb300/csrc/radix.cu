@@ -272,18 +272,25 @@ __global__ void __launch_bounds__(kThreads) k_big_hist(BigArgs a, const uint32_t
         int base = d.x + j * TILE;
         int cnt = min(TILE, d.y - j * TILE);
         uint32_t kr[IT];
+        auto count = [&](uint32_t k) {
+            atomicAdd(&h0[k & m0], 1u);
 #pragma unroll
-        for (int it = 0; it < IT; ++it) {
-            int i = it * kThreads + threadIdx.x;
-            kr[it] = i < cnt ? __ldg(key + base + i) : 0u;
-        }
+            for (int p = 0; p < 3; ++p) atomicAdd(&h[p][(k >> (w0 + 8 * p)) & 255u], 1u);
+        };
+        if (cnt == TILE) {  // full tile: no per-slot predicates
 #pragma unroll
-        for (int it = 0; it < IT; ++it) {
-            if (it * kThreads + (int)threadIdx.x < cnt) {
-                atomicAdd(&h0[kr[it] & m0], 1u);
+            for (int it = 0; it < IT; ++it) kr[it] = __ldg(key + base + it * kThreads + threadIdx.x);
 #pragma unroll
-                for (int p = 0; p < 3; ++p) atomicAdd(&h[p][(kr[it] >> (w0 + 8 * p)) & 255u], 1u);
+            for (int it = 0; it < IT; ++it) count(kr[it]);
+        } else {
+#pragma unroll
+            for (int it = 0; it < IT; ++it) {
+                int i = it * kThreads + threadIdx.x;
+                kr[it] = i < cnt ? __ldg(key + base + i) : 0u;
             }
+#pragma unroll
+            for (int it = 0; it < IT; ++it)
+                if (it * kThreads + (int)threadIdx.x < cnt) count(kr[it]);
         }
         __syncthreads();
         uint32_t* g = h4 + (size_t)s * kH4;
@@ -422,17 +429,29 @@ __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass0(Bi
         const int src = j * TILE;
         const int n = min(TILE, d.y - j * TILE);
         uint32_t kr[IT], rk[IT];
-        // keys to registers and values to shared memory, all in flight at once
+        // keys to registers and values to shared memory, all in flight at
+        // once, then the ranking; full tiles without per-slot predicates
+        if (n == TILE) {
 #pragma unroll
-        for (int it = 0; it < IT; ++it) {
-            int i = (int)w * WSPAN + it * 32 + (int)ln;
-            kr[it] = i < n ? __ldcs(sk + src + i) : 0u;
-            if (i < n) cp_async4(vst + i, sv + src + i);
-        }
+            for (int it = 0; it < IT; ++it) {
+                int i = (int)w * WSPAN + it * 32 + (int)ln;
+                kr[it] = __ldcs(sk + src + i);
+                cp_async4(vst + i, sv + src + i);
+            }
 #pragma unroll
-        for (int it = 0; it < IT; ++it) {
-            int i = (int)w * WSPAN + it * 32 + (int)ln;
-            rk[it] = i < n ? atomicAdd(&cnt[kr[it] & m0], 1u) : 0u;
+            for (int it = 0; it < IT; ++it) rk[it] = atomicAdd(&cnt[kr[it] & m0], 1u);
+        } else {
+#pragma unroll
+            for (int it = 0; it < IT; ++it) {
+                int i = (int)w * WSPAN + it * 32 + (int)ln;
+                kr[it] = i < n ? __ldcs(sk + src + i) : 0u;
+                if (i < n) cp_async4(vst + i, sv + src + i);
+            }
+#pragma unroll
+            for (int it = 0; it < IT; ++it) {
+                int i = (int)w * WSPAN + it * 32 + (int)ln;
+                rk[it] = i < n ? atomicAdd(&cnt[kr[it] & m0], 1u) : 0u;
+            }
         }
         __syncthreads();
         {
