@@ -1048,7 +1048,7 @@ void sort_groups(Storage* S, const int* hc, int A, const int* d_A, uint32_t* key
         QZ_LAUNCH(S, st, "k_sort_small", 4ll * A + 16ll * small_el,
                   k_sort_small<<<grid_for(A, kThreads, sms * 16), kThreads, 0, st>>>(d_A, G, key, W));
     sort_medium_groups(S, f.list_med, cnt + CNT_MED, hc[CNT_MED], hc[CNT_MED_ELEMS], key, W, key, W, st);
-    sort_tile_groups(S, f.list_tile, cnt + CNT_TILE, hc[CNT_TILE], hc[CNT_TILE_ELEMS], key, W, key, W, st);
+    sort_tile_groups(S, f.list_tile, cnt + CNT_TILE, hc[CNT_TILE], hc[CNT_TILE_ELEMS], key, W, key, W, key_bits, st);
     sort_big_groups(S, f.list_large, cnt + CNT_LARGE, hc[CNT_LARGE], hc[CNT_LARGE_ELEMS], key, W, key_bits, st);
 }
 

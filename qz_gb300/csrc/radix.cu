@@ -37,17 +37,25 @@ constexpr unsigned long long kFlagAgg = 1ull << 32;
 constexpr unsigned long long kFlagInc = 2ull << 32;
 constexpr unsigned kSpinLimit = 1u << 24;
 
+// Pass-0 bins at most (an 11-bit first digit) and digit-count words per
+// listed group of the large-group sort (pass 0's bins, then 256 per later pass).
+constexpr int kH0 = 2048;            // pass-0 bins at most (11 bits)
+constexpr int kH4 = kH0 + 3 * 256;   // digit-count words per group
+
 // ------------------------------------------------------------------ one-tile groups
 
-// One CTA per group of kTileMin..kOT slots: stable 8-bit passes in shared
-// memory (warp match-based ranks; ping-pong key/value buffers).  Each warp
-// takes an equal contiguous share of the group (a multiple of 32 slots), and
-// digits that are equal across the whole group are skipped.  The group is
-// read from (skey, sval) and written to (key, val) at the same slots; the two
-// may be the same arrays.
+// One CTA per group of kTileMin..kOT slots, every pass in shared memory
+// (ping-pong key/value buffers).  The digit layout is the large-group sort's:
+// pass 0 takes the low w0 bits (8..11) and needs no stability, so it ranks
+// with shared-memory atomics over 2^w0 bins (the per-warp counter array
+// doubles as them); passes 1..3 are stable 8-bit passes with warp
+// match-based ranks.  Each warp takes an equal contiguous share of the group
+// (a multiple of 32 slots), and digits that are equal across the whole group
+// are skipped.  The group is read from (skey, sval) and written to (key, val)
+// at the same slots; the two may be the same arrays.
 __global__ void __launch_bounds__(kThreads) k_tile_sort(const int2* __restrict__ list, const int* __restrict__ d_count,
                                                         const uint32_t* skey, const int* sval, uint32_t* key,
-                                                        int* val) {
+                                                        int* val, int w0) {
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t* k0 = reinterpret_cast<uint32_t*>(smem);
     int* v0 = reinterpret_cast<int*>(k0 + kOT);
@@ -95,8 +103,60 @@ __global__ void __launch_bounds__(kThreads) k_tile_sort(const int2* __restrict__
         int* vs = v0;
         uint32_t* kd = k1;
         int* vd = v1;
-        for (int pass = 0; pass < 4; ++pass) {
-            const int shift = 8 * pass;
+        const uint32_t m0 = (1u << w0) - 1u;
+        if (diff & m0) {
+            // pass 0: unstable, shared atomics over 2^w0 bins
+            uint32_t* bins = &wcnt[0][0];
+            const int nbins = 1 << w0, per = nbins / kThreads;
+            for (int i = threadIdx.x; i < nbins; i += kThreads) bins[i] = 0;
+            __syncthreads();
+            uint32_t rk[kOItems];
+#pragma unroll
+            for (int it = 0; it < kOItems; ++it) {
+                const int i = (int)w * span + it * 32 + (int)ln;
+                if (it < nit && i < len) rk[it] = atomicAdd(&bins[ks[i] & m0], 1u);
+            }
+            __syncthreads();
+            {
+                // this thread's run of `per` consecutive bins
+                uint32_t c[kH0 / kThreads];
+                uint32_t sum = 0;
+#pragma unroll
+                for (int q = 0; q < kH0 / kThreads; ++q) {
+                    c[q] = q < per ? bins[threadIdx.x * per + q] : 0u;
+                    sum += c[q];
+                }
+                uint32_t tot;
+                uint32_t off = block_excl_sum(sum, sh, &tot);
+#pragma unroll
+                for (int q = 0; q < kH0 / kThreads; ++q) {
+                    if (q < per) {
+                        bins[threadIdx.x * per + q] = off;
+                        off += c[q];
+                    }
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int it = 0; it < kOItems; ++it) {
+                const int i = (int)w * span + it * 32 + (int)ln;
+                if (it < nit && i < len) {
+                    const uint32_t kv = ks[i];
+                    const uint32_t p = bins[kv & m0] + rk[it];
+                    kd[p] = kv;
+                    vd[p] = vs[i];
+                }
+            }
+            __syncthreads();
+            uint32_t* tk = ks;
+            ks = kd;
+            kd = tk;
+            int* tv = vs;
+            vs = vd;
+            vd = tv;
+        }
+        for (int pass = 1; pass < 4; ++pass) {
+            const int shift = w0 + 8 * (pass - 1);
             if (((diff >> shift) & 255u) == 0) continue;
 #pragma unroll
             for (int q = 0; q < kWarps; ++q) wcnt[q][threadIdx.x] = 0;
@@ -166,8 +226,6 @@ __global__ void __launch_bounds__(kThreads) k_tile_sort(const int2* __restrict__
 // of a 25 MiB block need 26) therefore sort in three passes.  Per group the
 // digit counts sit in kH4 words: pass 0's 2^w0 counts, then 256 per later pass.
 // The look-back tile holds TILE slots (2048, 4096 or 8192; a tuning knob).
-constexpr int kH0 = 2048;            // pass-0 bins at most (11 bits)
-constexpr int kH4 = kH0 + 3 * 256;   // digit-count words per group
 
 __device__ __forceinline__ int digit_shift(int pass, int w0) { return pass == 0 ? 0 : w0 + 8 * (pass - 1); }
 __device__ __forceinline__ int h4_row(int pass) { return pass == 0 ? 0 : kH0 + 256 * (pass - 1); }
@@ -663,9 +721,20 @@ int grid_cap(long long work, int per_cta, int cap) {
 size_t tile_sort_smem() { return (size_t)kOT * 16 + sizeof(uint32_t) * kWarps * 256; }
 size_t big_hist_words() { return kH4; }
 
+namespace {
+// Width of pass 0's digit for keys of key_bits bits: wide enough that three
+// 8-bit passes above it cover the key, up to the tuned maximum; 8 otherwise.
+int first_digit_bits(int key_bits, int max_bits) {
+    if (key_bits > 24 && key_bits <= 16 + max_bits) return key_bits - 16;
+    return 8;
+}
+}  // namespace
+
 void sort_tile_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
-                      const uint32_t* skey, const int* sval, uint32_t* key, int* val, cudaStream_t st) {
+                      const uint32_t* skey, const int* sval, uint32_t* key, int* val, int key_bits,
+                      cudaStream_t st) {
     if (host_count <= 0) return;
+    const int w0 = first_digit_bits(key_bits, S->tune.first_digit_max);
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(k_tile_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_sort_smem());
@@ -673,7 +742,7 @@ void sort_tile_groups(Storage* S, const int2* list, const int* d_count, int host
     }
     QZ_LAUNCH(S, st, "k_tile_sort", 16 * elems,
               k_tile_sort<<<grid_cap(host_count, 1, S->sms * S->tune.tile_ctas_per_sm), kThreads, tile_sort_smem(),
-                            st>>>(list, d_count, skey, sval, key, val));
+                            st>>>(list, d_count, skey, sval, key, val, w0));
 }
 
 namespace {
@@ -693,13 +762,6 @@ void big_plan(Storage* S, const int2* list, const int* d_count, int host_count, 
         scan_exclusive(S, f.ltc, f.ltbase, 0, d_count, (uint32_t*)(cnt + CNT_LTILES), st);
         scan_exclusive(S, f.llen, f.lwbase, 0, d_count, nullptr, st);
     }
-}
-
-// Width of pass 0's digit for keys of key_bits bits: wide enough that three
-// 8-bit passes above it cover the key, up to the tuned maximum; 8 otherwise.
-int first_digit_bits(int key_bits, int max_bits) {
-    if (key_bits > 24 && key_bits <= 16 + max_bits) return key_bits - 16;
-    return 8;
 }
 
 template <int TILE>

@@ -31,8 +31,11 @@ struct BigBuffers {
 // elems are host copies (or bounds) of the group and slot counts; d_count is
 // the device count the kernels read.
 // Groups of medium_max+1 .. kOT slots (one CTA each, all passes in shared memory).
+// key_bits: the keys are below 2^key_bits (sets the first digit's width, as
+// for the large groups).
 void sort_tile_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
-                      const uint32_t* skey, const int* sval, uint32_t* key, int* val, cudaStream_t st);
+                      const uint32_t* skey, const int* sval, uint32_t* key, int* val, int key_bits,
+                      cudaStream_t st);
 // Groups of 17..64 slots (one warp each, rank by count; fwd.cu).
 void sort_rbc_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
                      const uint32_t* skey, const int* sval, uint32_t* key, int* val, cudaStream_t st);
