@@ -441,11 +441,12 @@ __global__ void __launch_bounds__(kThreads) k_sort_straddle(const int* __restric
     }
 }
 
-// 65..512 slots: stable LSD radix sort by one warp.  Lane l holds slots
-// it*32 + l in registers; each pass ranks them (warp matches, 256 digit
-// counters in shared memory), scatters (key, suffix) pairs into the warp's one
-// shared buffer and reads them back in the new order.  8-bit digits that are
-// equal across the whole group are skipped.
+// 65..512 slots: LSD radix sort by one warp.  Lane l holds slots it*32 + l
+// in registers; each pass ranks them (256 digit counters in shared memory),
+// scatters (key, suffix) pairs into the warp's one shared buffer and reads them
+// back in the new order.  8-bit digits that are equal across the whole group
+// are skipped.  The first pass run ranks with shared atomics (equal keys may
+// leave in any order); the later ones are stable (warp matches).
 constexpr size_t kMedWarpSmem = (size_t)kMedMax * 8 + 256 * 4;
 
 __device__ __forceinline__ void warp_radix_sort(const uint32_t* skey, const int* sW, uint32_t* key, int* W, int s,
@@ -476,6 +477,7 @@ __device__ __forceinline__ void warp_radix_sort(const uint32_t* skey, const int*
         kand &= __shfl_xor_sync(0xffffffffu, kand, d);
     }
     const uint32_t diff = kor ^ kand;
+    bool first = true;  // the first pass run needs no stability
     for (int pass = 0; pass < 4; ++pass) {
         const int sh = 8 * pass;
         if (((diff >> sh) & 255u) == 0) continue;
@@ -488,15 +490,22 @@ __device__ __forceinline__ void warp_radix_sort(const uint32_t* skey, const int*
             if (it < nit) {
                 const bool valid = it * 32 + ln < len;
                 const unsigned dg = valid ? (kr[it] >> sh) & 255u : 256u;
-                const unsigned peers = __match_any_sync(0xffffffffu, dg);
-                const unsigned before = __popc(peers & lt);
-                const uint32_t prev = valid ? cnt[dg] : 0u;
-                __syncwarp();
-                if (valid && before == 0) cnt[dg] = prev + __popc(peers);
-                __syncwarp();
-                rk[it] = prev + before;
+                if (first) {
+                    // equal keys may leave in any order: shared atomics rank
+                    rk[it] = valid ? atomicAdd(&cnt[dg], 1u) : 0u;
+                } else {
+                    const unsigned peers = __match_any_sync(0xffffffffu, dg);
+                    const unsigned before = __popc(peers & lt);
+                    const uint32_t prev = valid ? cnt[dg] : 0u;
+                    __syncwarp();
+                    if (valid && before == 0) cnt[dg] = prev + __popc(peers);
+                    __syncwarp();
+                    rk[it] = prev + before;
+                }
             }
         }
+        __syncwarp();
+        first = false;
         {
             // exclusive scan of the counters, eight consecutive digits per lane
             uint4 a = reinterpret_cast<uint4*>(cnt)[2 * ln], b = reinterpret_cast<uint4*>(cnt)[2 * ln + 1];
