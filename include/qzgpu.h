@@ -155,9 +155,14 @@ int qzgpu_storage_round_counts(const qzgpu_storage *storage, long long *active, 
  *   "round_pipeline"                  forward doubling rounds: 0 each round issued after
  *                                     its counts are read back, 1 issued one round ahead
  *                                     with launch shapes from bounds
- *   "lookback_test"                   1: failure-detection test (forward calls fail with
+ *   "split_lookback"                  split after each group sort: 0 count, scan and
+ *                                     apply passes (default), 1 one pass with decoupled
+ *                                     look-back (less kernel time on one lane, slower
+ *                                     when lanes overlap)
+ *   "lookback_test"                   failure-detection test: forward calls fail with
  *                                     QZGPU_TIMEOUT through a bounded look-back wait that
- *                                     runs out; no GPU fault); 0: off (default)
+ *                                     runs out, no GPU fault (1: in the radix sort, 2: in
+ *                                     the one-pass split); 0: off (default)
  * get_param also answers "lanes".  Returns 0 / the value, or QZGPU_BAD_PARAMETER
  * for an unknown name or an out-of-range value.  No counterpart in libbsc. */
 int qzgpu_storage_set_param(qzgpu_storage *storage, const char *name, long long value);

@@ -30,6 +30,7 @@ SPACE = {
     "big_tile": [2048, 4096, 8192],
     "radix_first_bits": [8, 11],
     "round_pipeline": [0, 1],
+    "split_lookback": [0, 1],
 }
 
 

@@ -25,21 +25,25 @@ constexpr int kOT = 4096;        // one CTA sorts a group of up to kOT slots; lo
 constexpr int kInitTile = 4096;  // text positions per tile of the per-block passes
 constexpr int kMaxRounds = 40;   // prefix doubling needs <= 31 rounds for n < 2^31
 
-// Device counters (int32 slots of Storage::counters).
+// Device counters (int32 slots of Storage::counters).  The ones a split
+// writes are contiguous, so that one memset clears them before it.
 enum Counter {
-    CNT_ACTIVE = 0,  // suffixes still in non-singleton groups (two slots: 0 and 6,
+    CNT_ACTIVE = 0,  // suffixes still in non-singleton groups (two slots: 0 and 1,
                      // a split reads one and writes the other)
-    CNT_MED = 2,     // descriptor counts of the listed classes
-    CNT_LARGE = 3,
-    CNT_LTILES = 4,  // tiles of the large-group radix sort
-    CNT_ACTIVE_ALT = 6,
-    CNT_MED_ELEMS = 8,  // slots covered by each listed class
-    CNT_TILE = 10,
-    CNT_TILE_ELEMS = 11,
-    CNT_TICKET = 12,    // tile tickets of a look-back radix pass
-    CNT_PAIR = 13,      // groups of 17..64 slots (rank-by-count class)
-    CNT_PAIR_ELEMS = 14,
-    CNT_LARGE_ELEMS = 9,
+    CNT_ACTIVE_ALT = 1,
+    CNT_LTILES = 2,  // tiles of the large-group radix sort
+    CNT_TICKET = 3,  // tile tickets of a look-back radix pass
+    CNT_SPLIT_FIRST = 4,
+    CNT_MED = 4,     // descriptor counts of the listed classes
+    CNT_LARGE = 5,
+    CNT_MED_ELEMS = 6,  // slots covered by each listed class
+    CNT_LARGE_ELEMS = 7,
+    CNT_TILE = 8,
+    CNT_TILE_ELEMS = 9,
+    CNT_PAIR = 10,      // groups of 17..64 slots (rank-by-count class)
+    CNT_PAIR_ELEMS = 11,
+    CNT_SPLIT_TICKET = 12,  // warp-tile tickets of a one-pass split
+    CNT_SPLIT_END = 13,
     CNT_SLOTS = 16,
 };
 
@@ -69,6 +73,7 @@ struct FwdBuffers {
     uint32_t* p_surv;  // split: per 256-slot warp tile
     int* p_sub;
     int* p_grp;
+    unsigned long long* split_status;  // one-pass split: look-back words per warp tile
     uint32_t* c_surv;  // split: per scan chunk
     int* c_sub;
     int* c_grp;
@@ -95,9 +100,11 @@ struct Tune {
     int big_tile = 4096;       // slots per look-back tile of the large-group sort (2048, 4096, 8192)
     int first_digit_max = 11;  // widest first radix digit of the large-group sort (8..11 bits)
     int round_pipeline = 0;    // forward rounds: 0 issued after the host reads their counts, 1 issued ahead
-    // failure-detection test: in the first stable radix pass the second tile
-    // of every group publishes nothing and look-back waits give up after 4096
-    // polls, so the tiles after it report QZGPU_TIMEOUT (no GPU fault)
+    int split_lookback = 0;    // split: 0 count + scan + apply passes, 1 one pass with decoupled look-back
+    // failure-detection test: 1: in the first stable radix pass the second
+    // tile of every group publishes nothing; 2: in every one-pass split the
+    // second tile publishes nothing.  Look-back waits then give up after
+    // 4096 polls, so the tiles after it report QZGPU_TIMEOUT (no GPU fault)
     int lookback_test = 0;
 };
 

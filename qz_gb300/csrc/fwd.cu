@@ -646,7 +646,8 @@ struct SplitArgs {
     int* p_grp;
     int write_rank;    // kRankNone / kRankChanged / kRankAll
     int medium_max;    // longest group listed for the one-warp sort
-    const DevStatus* st;
+    int n;             // suffix-array entries (bound of the SA stores)
+    DevStatus* st;
 };
 
 // Lane l of a warp tile holds the 8 consecutive slots base + 8l .. base + 8l + 7,
@@ -804,14 +805,6 @@ __global__ void __launch_bounds__(kThreads) k_pscan_top(SplitArgs a, uint32_t* _
     }
     if (threadIdx.x == 0) {
         *a.A_next = (int)carry;
-        a.counters[CNT_MED] = 0;
-        a.counters[CNT_PAIR] = 0;
-        a.counters[CNT_PAIR_ELEMS] = 0;
-        a.counters[CNT_TILE] = 0;
-        a.counters[CNT_LARGE] = 0;
-        a.counters[CNT_MED_ELEMS] = 0;
-        a.counters[CNT_TILE_ELEMS] = 0;
-        a.counters[CNT_LARGE_ELEMS] = 0;
     }
 }
 
@@ -846,14 +839,6 @@ __global__ void __launch_bounds__(kThreads) k_pscan_single(SplitArgs a) {
     }
     if (threadIdx.x == 0) {
         *a.A_next = (int)carry;
-        a.counters[CNT_PAIR] = 0;
-        a.counters[CNT_PAIR_ELEMS] = 0;
-        a.counters[CNT_MED] = 0;
-        a.counters[CNT_TILE] = 0;
-        a.counters[CNT_LARGE] = 0;
-        a.counters[CNT_MED_ELEMS] = 0;
-        a.counters[CNT_TILE_ELEMS] = 0;
-        a.counters[CNT_LARGE_ELEMS] = 0;
     }
 }
 
@@ -888,6 +873,88 @@ __global__ void __launch_bounds__(kThreads) k_pscan_apply(SplitArgs a, const uin
     }
 }
 
+// A loaded warp tile's per-lane counts: survivors and finished suffixes among
+// the lane's slots with their inclusive scans over the lanes, the last
+// subgroup and group heads of the lanes before it, and the tile's totals.
+struct TileScan {
+    unsigned alive;
+    int lsurv, isurv, lsing, ising;
+    int xsub, xgrp;  // exclusive over the lanes (-1: none)
+    int tsurv, tsub, tgrp;
+};
+
+__device__ __forceinline__ TileScan tile_scan(const WarpTile& t, int first) {
+    const int ln = (int)lane_id();
+    TileScan s;
+    s.alive = t.valid & ~(t.sh & t.nsh);
+    s.lsurv = __popc(s.alive);
+    const int lsub = t.sh ? first + 31 - __clz(t.sh) : -1;
+    const int lgrp = t.gh ? first + 31 - __clz(t.gh) : -1;
+    s.isurv = warp_incl_sum(s.lsurv);
+    s.lsing = __popc(t.valid) - s.lsurv;
+    s.ising = warp_incl_sum(s.lsing);
+    const int isub = warp_incl_max(lsub), igrp = warp_incl_max(lgrp);
+    s.xsub = __shfl_up_sync(0xffffffffu, isub, 1);
+    s.xgrp = __shfl_up_sync(0xffffffffu, igrp, 1);
+    if (ln == 0) s.xsub = s.xgrp = -1;
+    s.tsurv = __shfl_sync(0xffffffffu, s.isurv, 31);
+    s.tsub = __shfl_sync(0xffffffffu, isub, 31);
+    s.tgrp = __shfl_sync(0xffffffffu, igrp, 31);
+    return s;
+}
+
+// The stores of one warp tile, given the survivors of the tiles before it
+// (dest) and the last subgroup and group heads before it (psub, pgrp).
+__device__ __forceinline__ void split_tile_apply(const SplitArgs& a, const WarpTile& t, const TileScan& s,
+                                                 int first, uint32_t dest, int psub, int pgrp, int2* st,
+                                                 unsigned long long pol) {
+    const int ln = (int)lane_id();
+    int ks = max(psub, s.xsub), kg = max(pgrp, s.xgrp);
+    int at = s.isurv - s.lsurv;   // this lane's first survivor, within the tile
+    int atf = s.ising - s.lsing;  // this lane's first finished suffix, within the tile
+#pragma unroll
+    for (int i = 0; i < kWI; ++i) {
+        if (!(t.valid >> i & 1u)) continue;
+        const int kk = first + i;
+        if (t.sh >> i & 1u) ks = kk;
+        if (t.gh >> i & 1u) kg = kk;
+        const int w = t.w[i], g = t.g[i];
+        const int rank = g + (ks - kg);
+        if (a.write_rank == kRankAll || (a.write_rank == kRankChanged && rank != g)) st_keep(a.R + w, rank, pol);
+        if (!(s.alive >> i & 1u)) {
+            st[kWT - 1 - atf] = make_int2(g + (kk - kg), w);
+            ++atf;
+            continue;
+        }
+        st[at] = make_int2(w, rank);
+        const uint32_t d = dest + (uint32_t)at;
+        ++at;
+        // a surviving subgroup longer than kSmallMax ends here: list it by class
+        const int L = kk - ks + 1;
+        if ((t.nsh >> i & 1u) && L > kSmallMax) {
+            const int cls = L <= 64 ? 3 : (L <= a.medium_max ? 0 : (L <= kOT ? 1 : 2));
+            const int ci = cls == 0 ? CNT_MED : (cls == 1 ? CNT_TILE : (cls == 2 ? CNT_LARGE : CNT_PAIR));
+            const int ce = cls == 0 ? CNT_MED_ELEMS
+                                    : (cls == 1 ? CNT_TILE_ELEMS : (cls == 2 ? CNT_LARGE_ELEMS : CNT_PAIR_ELEMS));
+            int2* list = cls == 0 ? a.list_med : (cls == 1 ? a.list_tile : (cls == 2 ? a.list_large : a.list_rbc));
+            list[atomicAdd(&a.counters[ci], 1)] = make_int2((int)d - L + 1, L);
+            atomicAdd(&a.counters[ce], L);
+        }
+    }
+    __syncwarp();
+    for (int j = ln; j < s.tsurv; j += 32) {
+        const int2 v = st[j];
+        __stcs(a.Wn + dest + j, v.x);
+        __stcs(a.Gn + dest + j, v.y);
+    }
+    const int fin = __shfl_sync(0xffffffffu, s.ising, 31);
+    for (int j = ln; j < fin; j += 32) {
+        const int2 v = st[kWT - 1 - j];
+        if ((unsigned)v.x < (unsigned)a.n) a.SA[v.x] = v.y;
+    }
+    __syncwarp();
+}
+
 __global__ void __launch_bounds__(kThreads, 5) k_split_apply(SplitArgs a) {
     // a warp tile's survivors (from the front) and finished suffixes (from the
     // back), staged so that both leave as coalesced rows
@@ -896,72 +963,176 @@ __global__ void __launch_bounds__(kThreads, 5) k_split_apply(SplitArgs a) {
     int A = *a.A;
     int ntiles = (A + kWT - 1) / kWT;
     int nwarps = gridDim.x * kWarps;
-    const int ln = (int)lane_id();
     int2* st = stage[warp_id()];
     const unsigned long long pol = l2_keep_policy();
     for (int tile = blockIdx.x * kWarps + (int)warp_id(); tile < ntiles; tile += nwarps) {
         const int base = tile * kWT;
         WarpTile t;
         wt_load<true>(a, A, base, t);
-        const int first = base + kWI * ln;
-        const uint32_t dest = a.p_surv[tile];
-        // this lane's survivors, last subgroup head and last group head, and
-        // the exclusive values of the lanes before it
-        const unsigned alive = t.valid & ~(t.sh & t.nsh);
-        const int lsurv = __popc(alive);
-        const int lsub = t.sh ? first + 31 - __clz(t.sh) : -1;
-        const int lgrp = t.gh ? first + 31 - __clz(t.gh) : -1;
-        const int isurv = warp_incl_sum(lsurv);
-        const int lsing = __popc(t.valid) - lsurv;
-        const int ising = warp_incl_sum(lsing);
-        int atf = ising - lsing;  // this lane's first finished suffix, within the tile
-        int isub = warp_incl_max(lsub), igrp = warp_incl_max(lgrp);
-        int xsub = __shfl_up_sync(0xffffffffu, isub, 1), xgrp = __shfl_up_sync(0xffffffffu, igrp, 1);
-        if (ln == 0) xsub = xgrp = -1;
-        int ks = max(a.p_sub[tile], xsub), kg = max(a.p_grp[tile], xgrp);
-        int at = isurv - lsurv;  // this lane's first survivor, within the tile
+        const int first = base + kWI * (int)lane_id();
+        const TileScan s = tile_scan(t, first);
+        split_tile_apply(a, t, s, first, a.p_surv[tile], a.p_sub[tile], a.p_grp[tile], st, pol);
+    }
+}
+
+// ------------------------------------------------------------------ one-pass split
+//
+// The count, scan and apply passes above in one pass over CTA tiles of
+// kWarps warp tiles (2048 slots).  CTAs take tiles by ticket, in order.  Each
+// warp loads and scans its warp tile; warp 0 combines the warps' totals
+// (survivors, last subgroup head, last group head), publishes the tile's
+// totals, looks back over the tiles before it for their exclusive values
+// (decoupled look-back, one lane per earlier tile, 32 at a time) and
+// publishes its inclusive values; then every warp applies its warp tile.
+// Each total has its own status word per tile: the value in the low 32 bits,
+// the state (1 aggregate, 2 inclusive) in bits 32-33 and the launch's epoch
+// above, so nothing is cleared between splits.  Heads are stored plus one,
+// so that zero means none.  A tile waits only on tiles of earlier tickets,
+// which resident CTAs hold and publish before they wait; a wait that exceeds
+// its limit records QZGPU_TIMEOUT, and the tile then stores nothing (its
+// inclusive values are still published, so that the tiles after it finish).
+
+constexpr int kCT = kWarps * kWT;  // slots per CTA tile of the one-pass split
+
+struct SplitLookBack {
+    unsigned long long* status;  // 4 words per CTA tile (3 used)
+    unsigned* ticket;
+    unsigned epoch;
+    unsigned spin_limit;
+    int silent_tile;  // failure-detection test: this tile publishes nothing (-1: none)
+};
+
+constexpr unsigned kSplitSpinLimit = 1u << 24;  // polls of 32 ns and more
+constexpr unsigned long long kSplitAgg = 1ull << 32;
+constexpr unsigned long long kSplitInc = 2ull << 32;
+
+__device__ __forceinline__ bool split_ready(unsigned long long v, unsigned epoch) {
+    return (unsigned)(v >> 34) == epoch && (v & (3ull << 32)) != 0;
+}
+
+// Exclusive totals of the tiles before `tile` (one warp): ex[0] survivors
+// (sum), ex[1] and ex[2] last subgroup and group head plus one (max).  False
+// if a wait ran out.
+__device__ __forceinline__ bool split_look_back(const SplitLookBack& lb, int tile, uint32_t (&ex)[3],
+                                                DevStatus* st) {
+    const int ln = (int)lane_id();
+    const unsigned long long none = ((unsigned long long)lb.epoch << 34) | kSplitInc;  // inclusive zero
+    unsigned done = 0;  // bit c: total c found
+    for (int p = tile - 1; done != 7u; p -= 32) {
+        const int q = p - ln;  // this lane's tile
+        const volatile unsigned long long* w = lb.status + 4ll * (q < 0 ? 0 : q);
+        unsigned long long v[3];
 #pragma unroll
-        for (int i = 0; i < kWI; ++i) {
-            if (!(t.valid >> i & 1u)) continue;
-            const int kk = first + i;
-            if (t.sh >> i & 1u) ks = kk;
-            if (t.gh >> i & 1u) kg = kk;
-            const int w = t.w[i], g = t.g[i];
-            const int rank = g + (ks - kg);
-            if (a.write_rank == kRankAll || (a.write_rank == kRankChanged && rank != g)) st_keep(a.R + w, rank, pol);
-            if (!(alive >> i & 1u)) {
-                st[kWT - 1 - atf] = make_int2(g + (kk - kg), w);
-                ++atf;
-                continue;
+        for (int c = 0; c < 3; ++c) v[c] = (q >= 0 && !(done >> c & 1u)) ? w[c] : none;
+        unsigned spins = 0;
+        while (!(split_ready(v[0], lb.epoch) && split_ready(v[1], lb.epoch) && split_ready(v[2], lb.epoch)) &&
+               spins < lb.spin_limit) {
+            __nanosleep(32);
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                if (!split_ready(v[c], lb.epoch)) v[c] = w[c];
+            ++spins;
+        }
+        if (__any_sync(0xffffffffu, spins >= lb.spin_limit)) {
+            if (ln == 0) report(st, QZGPU_TIMEOUT, 21, tile);
+            return false;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if (done >> c & 1u) continue;
+            // lanes up to the nearest tile with an inclusive value contribute
+            const unsigned inc = __ballot_sync(0xffffffffu, (v[c] & kSplitInc) != 0);
+            const int lim = inc ? __ffs(inc) - 1 : 31;
+            const unsigned x = ln <= lim ? (unsigned)v[c] : 0u;
+            if (c == 0)
+                ex[0] += __reduce_add_sync(0xffffffffu, x);
+            else
+                ex[c] = max(ex[c], __reduce_max_sync(0xffffffffu, x));
+            if (inc) done |= 1u << c;
+        }
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(kThreads, 5) k_split(SplitArgs a, SplitLookBack lb) {
+    __shared__ int2 stage[kWarps][kWT];
+    __shared__ uint32_t s_tot[3][kWarps];  // per warp tile: survivors, subgroup head + 1, group head + 1
+    __shared__ uint32_t s_ex[3];           // the CTA tile's exclusive totals
+    __shared__ int s_tile, s_ok;
+    if (failed(a.st)) return;  // suffixes may be duplicated or stale
+    const int A = *a.A;
+    const int ntiles = (A + kCT - 1) / kCT;
+    if (ntiles == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) *a.A_next = 0;
+        return;
+    }
+    const int ln = (int)lane_id(), wp = (int)warp_id();
+    int2* st = stage[wp];
+    const unsigned long long pol = l2_keep_policy();
+    const unsigned long long ep = (unsigned long long)lb.epoch << 34;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(lb.ticket, 1u);
+        __syncthreads();
+        const int tile = s_tile;
+        if (tile >= ntiles) return;
+        const int base = tile * kCT + wp * kWT;
+        const int first = base + kWI * ln;
+        WarpTile t;
+        if (base < A) {
+            wt_load<true>(a, A, base, t);
+        } else {
+            t.valid = t.gh = t.sh = t.nsh = 0;
+        }
+        const TileScan s = tile_scan(t, first);
+        if (ln == 0) {
+            s_tot[0][wp] = (uint32_t)s.tsurv;
+            s_tot[1][wp] = (uint32_t)(s.tsub + 1);
+            s_tot[2][wp] = (uint32_t)(s.tgrp + 1);
+        }
+        __syncthreads();
+        if (wp == 0) {
+            // the CTA tile's totals and each warp tile's exclusive values within it
+            const bool in = ln < kWarps;
+            const uint32_t vs = in ? s_tot[0][ln] : 0u, vh = in ? s_tot[1][ln] : 0u, vg = in ? s_tot[2][ln] : 0u;
+            const uint32_t is = warp_incl_sum(vs);
+            const uint32_t ih = (uint32_t)warp_incl_max((int)vh), ig = (uint32_t)warp_incl_max((int)vg);
+            const uint32_t agg0 = __shfl_sync(0xffffffffu, is, kWarps - 1);
+            const uint32_t agg1 = __shfl_sync(0xffffffffu, ih, kWarps - 1);
+            const uint32_t agg2 = __shfl_sync(0xffffffffu, ig, kWarps - 1);
+            const uint32_t xh = __shfl_up_sync(0xffffffffu, ih, 1), xg = __shfl_up_sync(0xffffffffu, ig, 1);
+            if (in) {
+                s_tot[0][ln] = is - vs;
+                s_tot[1][ln] = ln == 0 ? 0u : xh;
+                s_tot[2][ln] = ln == 0 ? 0u : xg;
             }
-            st[at] = make_int2(w, rank);
-            const uint32_t d = dest + (uint32_t)at;
-            ++at;
-            // a surviving subgroup longer than kSmallMax ends here: list it by class
-            const int L = kk - ks + 1;
-            if ((t.nsh >> i & 1u) && L > kSmallMax) {
-                const int cls = L <= 64 ? 3 : (L <= a.medium_max ? 0 : (L <= kOT ? 1 : 2));
-                const int ci = cls == 0 ? CNT_MED : (cls == 1 ? CNT_TILE : (cls == 2 ? CNT_LARGE : CNT_PAIR));
-                const int ce = cls == 0 ? CNT_MED_ELEMS
-                                        : (cls == 1 ? CNT_TILE_ELEMS : (cls == 2 ? CNT_LARGE_ELEMS : CNT_PAIR_ELEMS));
-                int2* list = cls == 0 ? a.list_med : (cls == 1 ? a.list_tile : (cls == 2 ? a.list_large : a.list_rbc));
-                list[atomicAdd(&a.counters[ci], 1)] = make_int2((int)d - L + 1, L);
-                atomicAdd(&a.counters[ce], L);
+            const uint32_t agg = ln == 0 ? agg0 : (ln == 1 ? agg1 : agg2);
+            volatile unsigned long long* my = lb.status + 4ll * tile + ln;
+            const bool pub = ln < 3 && tile != lb.silent_tile;
+            uint32_t ex[3] = {0u, 0u, 0u};
+            bool ok = true;
+            if (tile > 0) {
+                if (pub) *my = ep | kSplitAgg | agg;
+                ok = split_look_back(lb, tile, ex, a.st);
+            }
+            const uint32_t mine = ln == 0 ? ex[0] : (ln == 1 ? ex[1] : ex[2]);
+            if (pub) *my = ep | kSplitInc | (ln == 0 ? mine + agg : max(mine, agg));
+            if (tile == ntiles - 1 && ln == 0) *a.A_next = (int)(ex[0] + agg0);
+            if (ln == 0) {
+                s_ex[0] = ex[0];
+                s_ex[1] = ex[1];
+                s_ex[2] = ex[2];
+                s_ok = ok;
             }
         }
-        __syncwarp();
-        const int tot = __shfl_sync(0xffffffffu, isurv, 31);
-        for (int j = ln; j < tot; j += 32) {
-            const int2 v = st[j];
-            __stcs(a.Wn + dest + j, v.x);
-            __stcs(a.Gn + dest + j, v.y);
+        __syncthreads();
+        if (s_ok && base < A) {
+            // survivors before a warp tile are at most its first slot
+            const uint32_t dest = min(s_ex[0] + s_tot[0][wp], (uint32_t)base);
+            const int psub = (int)max(s_ex[1], s_tot[1][wp]) - 1;
+            const int pgrp = (int)max(s_ex[2], s_tot[2][wp]) - 1;
+            split_tile_apply(a, t, s, first, dest, psub, pgrp, st, pol);
         }
-        const int fin = __shfl_sync(0xffffffffu, ising, 31);
-        for (int j = ln; j < fin; j += 32) {
-            const int2 v = st[kWT - 1 - j];
-            a.SA[v.x] = v.y;
-        }
-        __syncwarp();
+        __syncthreads();  // s_tile, s_tot and s_ex are rewritten by the next tile
     }
 }
 
@@ -1072,6 +1243,13 @@ void add_round(Storage* S, int r, long long a) {
 
 // One sub-batch: blocks laid out back to back from d_T, using the storage
 // arrays from position 0.  Accumulates round counts into S.
+// Launches whose stores of survivors, suffix-array entries and ranks are known
+// only once the next round's counts are read.
+bool split_store_kernel(const char* name) {
+    return strcmp(name, "k_split") == 0 || strcmp(name, "k_split_first") == 0 ||
+           strncmp(name, "k_split_apply", 13) == 0;
+}
+
 int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d_U, int* idx,
                  const int* aux_rate, int* aux_out, cudaStream_t st, int* rounds_out) {
     long long N = 0;
@@ -1157,6 +1335,12 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
     if (e == cudaSuccess) e = cudaMemsetAsync(S->blk_hist, 0, sizeof(uint32_t) * 256 * nb, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(S->status, 0, sizeof(DevStatus), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(S->blk_idx, 0xff, sizeof(int) * nb, st);
+    // look-back status words: this sub-batch's epochs are new, but the inverse
+    // reuses the memory, and a word it left could carry one of them
+    const size_t big_tiles = (size_t)N / 2048 + (size_t)N / 4097 + 4;
+    if (e == cudaSuccess) e = cudaMemsetAsync(f.status64, 0, sizeof(unsigned long long) * 256 * big_tiles, st);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(f.split_status, 0, sizeof(unsigned long long) * 4 * ((size_t)N / kWT + 2), st);
     if (e != cudaSuccess) return map_cuda_error(e);
 
     // ---- alphabet, initial keys
@@ -1210,9 +1394,29 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
         a.p_grp = f.p_grp;
         a.write_rank = rank_mode;
         a.medium_max = S->tune.medium_max;
+        a.n = (int)N;
         a.st = S->status;
-        int grid = grid_for((A + kWT - 1) / kWT, kWarps, S->sms * 8);
         long long tiles_n = (A + kWT - 1) / kWT;
+        // the class counters the split appends to (and its ticket) start at zero
+        if (!S->dry && e == cudaSuccess)
+            e = cudaMemsetAsync(S->counters + CNT_SPLIT_FIRST, 0, sizeof(int) * (CNT_SPLIT_END - CNT_SPLIT_FIRST), st);
+        if (S->tune.split_lookback) {
+            // key, group rank and suffix of every slot in; 24 bytes of status
+            // per tile out; the rest is added once the survivors are known
+            unsigned epoch = ++S->radix_epoch & 0x3fffffffu;
+            if (epoch == 0) epoch = ++S->radix_epoch & 0x3fffffffu;
+            const bool test = S->tune.lookback_test == 2;
+            SplitLookBack lb{f.split_status, reinterpret_cast<unsigned*>(S->counters + CNT_SPLIT_TICKET), epoch,
+                             test ? 4096u : kSplitSpinLimit, test ? 1 : -1};
+            const long long ctiles = (A + kCT - 1) / kCT;
+            const int grid = (int)std::max(1ll, std::min<long long>(ctiles, (long long)S->sms * 5));
+            QZ_LAUNCH(S, st, rank_mode == kRankNone ? "k_split_first" : "k_split", 12 * A + 24 * ctiles,
+                      k_split<<<grid, kThreads, 0, st>>>(a, lb));
+            cur ^= 1;
+            act ^= CNT_ACTIVE ^ CNT_ACTIVE_ALT;
+            return;
+        }
+        int grid = grid_for((A + kWT - 1) / kWT, kWarps, S->sms * 8);
         // count: key and group rank of every slot; 12 bytes of partials per tile
         QZ_LAUNCH(S, st, "k_split_count", 8 * A + 12 * tiles_n, k_split_count<<<grid, kThreads, 0, st>>>(a));
         if (tiles_n <= kPscanSingleMax) {
@@ -1329,7 +1533,7 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
     // profile record of the previous round's split apply (its survivors are
     // known one round later)
     int last_apply = -1;
-    if (S->profile && !S->prof_pending.empty() && strcmp(S->prof_pending.back().name, "k_split_apply_first") == 0)
+    if (S->profile && !S->prof_pending.empty() && split_store_kernel(S->prof_pending.back().name))
         last_apply = (int)S->prof_pending.size() - 1;
     int hb[CNT_SLOTS];
     for (;;) {
@@ -1374,7 +1578,7 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
             issue_round(round, hb, A);
             post((round + 1) & 1);
             last_apply = -1;
-            if (S->profile && !S->prof_pending.empty() && strcmp(S->prof_pending.back().name, "k_split_apply") == 0)
+            if (S->profile && !S->prof_pending.empty() && split_store_kernel(S->prof_pending.back().name))
                 last_apply = (int)S->prof_pending.size() - 1;
             A_prev = A;
             ++round;
@@ -1415,7 +1619,7 @@ int forward_core(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* 
                 } else {
                     rec.bytes = 0;
                 }
-                if (strncmp(rec.name, "k_split_apply", 13) == 0) last_apply = (int)i;
+                if (split_store_kernel(rec.name)) last_apply = (int)i;
             }
         }
         if (A == 0) break;  // the round just issued finds nothing to do

@@ -226,6 +226,7 @@ size_t layout(Storage* S, char* base, const Caps& c) {
     f.p_surv = cv.take<uint32_t>(wt);
     f.p_sub = cv.take<int>(wt);
     f.p_grp = cv.take<int>(wt);
+    f.split_status = cv.take<unsigned long long>(4 * wt);
     f.c_surv = cv.take<uint32_t>(1024);
     f.c_sub = cv.take<int>(1024);
     f.c_grp = cv.take<int>(1024);
@@ -682,8 +683,11 @@ int qzgpu_storage_set_param(qzgpu_storage* storage, const char* name, long long 
     } else if (k == "round_pipeline") {
         if (value < 0 || value > 1) return QZGPU_BAD_PARAMETER;
         each([&](Tune& t) { t.round_pipeline = (int)value; });
-    } else if (k == "lookback_test") {
+    } else if (k == "split_lookback") {
         if (value < 0 || value > 1) return QZGPU_BAD_PARAMETER;
+        each([&](Tune& t) { t.split_lookback = (int)value; });
+    } else if (k == "lookback_test") {
+        if (value < 0 || value > 2) return QZGPU_BAD_PARAMETER;
         each([&](Tune& t) { t.lookback_test = (int)value; });
     } else {
         return QZGPU_BAD_PARAMETER;
@@ -704,6 +708,7 @@ long long qzgpu_storage_get_param(const qzgpu_storage* storage, const char* name
     if (k == "big_tile") return t.big_tile;
     if (k == "radix_first_bits") return t.first_digit_max;
     if (k == "round_pipeline") return t.round_pipeline;
+    if (k == "split_lookback") return t.split_lookback;
     if (k == "lookback_test") return t.lookback_test;
     if (k == "lanes") return (long long)storage->lanes.size();
     return QZGPU_BAD_PARAMETER;

@@ -9,7 +9,7 @@ class FakeStorage:
     def __init__(self):
         self.p = {"fwd_sub_bytes": 64 << 20, "inv_sub_bytes": 64 << 20, "big_ctas_per_sm": 3,
                   "tile_ctas_per_sm": 3, "medium_max": 512, "ruler_stride_log2": 5, "big_tile": 4096,
-                  "radix_first_bits": 11, "round_pipeline": 0}
+                  "radix_first_bits": 11, "round_pipeline": 0, "split_lookback": 0}
 
     def set_param(self, k, v):
         self.p[k] = v

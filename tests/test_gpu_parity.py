@@ -152,15 +152,19 @@ def test_decode_wrong_index_does_not_hang(gpu):
         assert e.code == native.QZGPU_DATA_CORRUPT
 
 
-def test_lookback_wait_runs_out_without_fault(gpu, oracle):
-    # Failure detection: in the test mode one tile of every large group never
-    # publishes its look-back status, so the tiles behind it give up after a
-    # short bounded wait; the call returns QZGPU_TIMEOUT (no fault, no hang)
-    # and the same storage sorts correctly once the mode is off.
+@pytest.mark.parametrize("mode", [1, 2])
+def test_lookback_wait_runs_out_without_fault(gpu, oracle, mode):
+    # Failure detection: in the test mode one tile never publishes its
+    # look-back status (mode 1: a tile of every large group in the radix sort;
+    # mode 2: the second tile of every one-pass split), so the tiles
+    # behind it give up after a short bounded wait; the call returns
+    # QZGPU_TIMEOUT (no fault, no hang) and the same storage sorts correctly
+    # once the mode is off.
     rng = np.random.default_rng(5)
     blocks = [rng.integers(0, 256, 1 << 20).astype(np.uint8)]  # one 2^20-slot group at the start
     with bwt.Storage(len(blocks[0]), 1) as st:
-        st.set_param("lookback_test", 1)
+        st.set_param("split_lookback", 1 if mode == 2 else 0)
+        st.set_param("lookback_test", mode)
         with pytest.raises(native.QzGpuError) as e:
             st.encode_batch(blocks)
         assert e.value.code == native.QZGPU_TIMEOUT
@@ -170,11 +174,13 @@ def test_lookback_wait_runs_out_without_fault(gpu, oracle):
         assert idx == list(oidx)
         assert (us[0] == ous[0]).all()
         with pytest.raises(native.QzGpuError):
-            st.set_param("lookback_test", 2)
+            st.set_param("lookback_test", 3)
 
 
 @pytest.mark.parametrize("params", [
     {"medium_max": 64, "big_ctas_per_sm": 2, "ruler_stride_log2": 3, "round_pipeline": 1},
+    {"split_lookback": 1},
+    {"split_lookback": 1, "round_pipeline": 1, "medium_max": 128},
     {"medium_max": 512, "big_ctas_per_sm": 4, "fwd_sub_bytes": 1 << 20, "big_tile": 2048},
     {"medium_max": 128, "tile_ctas_per_sm": 1, "ruler_stride_log2": 7, "fwd_sub_bytes": 1 << 20,
      "inv_sub_bytes": 1 << 20, "big_tile": 8192, "radix_first_bits": 8, "round_pipeline": 1},
