@@ -159,7 +159,13 @@ int qzgpu_storage_round_counts(const qzgpu_storage *storage, long long *active, 
  *                                     apply passes (default), 1 one pass with decoupled
  *                                     look-back (less kernel time on one lane, slower
  *                                     when lanes overlap)
- *   "lookback_test"                   failure-detection test: forward calls fail with
+ *   "rank_mode"                       how a stable radix pass ranks a warp's digits:
+ *                                     0 warp match, 1 eight ballots, 2 a match on the
+ *                                     high four bits and four ballots (default)
+ *   "early_counts"                    stable radix pass: 1 (default) a tile publishes its
+ *                                     digit counts for the look-back before it ranks,
+ *                                     0 after
+ *   "lookback_test"                  failure-detection test: forward calls fail with
  *                                     QZGPU_TIMEOUT through a bounded look-back wait that
  *                                     runs out, no GPU fault (1: in the radix sort, 2: in
  *                                     the one-pass split); 0: off (default)

@@ -83,11 +83,32 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // Stable rank of this lane's item among the lanes of its warp that hold the
 // same digit, plus the running count of that digit (per-warp counters `cnt`,
 // one per digit): returns the count before this warp step plus the lanes with
-// the same digit below this one, and advances the count.  The lanes with the
-// same digit come from the warp match instruction; invalid lanes take no part.
+// the same digit below this one, and advances the count.  Invalid lanes take
+// no part.
+//
+// RANK picks how the lanes with the same 8-bit digit are found:
+//   0: one warp match instruction;
+//   1: eight ballots, one per digit bit (integer pipes, no match);
+//   2: a match on the high four bits and four ballots on the low four.
+template <int RANK = 0>
+__device__ __forceinline__ unsigned warp_digit_peers(unsigned dg, bool valid) {
+    if (RANK == 0) return __match_any_sync(0xffffffffu, valid ? dg : 0x10000u);
+    constexpr int LOW = RANK == 1 ? 8 : 4;
+    unsigned peers = RANK == 1 ? __ballot_sync(0xffffffffu, valid)
+                               : __match_any_sync(0xffffffffu, valid ? (dg >> 4) : 0x10000u);
+#pragma unroll
+    for (int b = 0; b < LOW; ++b) {
+        const unsigned bit = (dg >> b) & 1u;
+        const unsigned m = __ballot_sync(0xffffffffu, bit);
+        peers &= m ^ (bit - 1u);  // m where the bit is set, ~m where it is clear
+    }
+    return peers;
+}
+
+template <int RANK = 0>
 __device__ __forceinline__ uint32_t warp_digit_rank(unsigned dg, bool valid, uint32_t* cnt) {
     const unsigned lt = (1u << lane_id()) - 1u;
-    const unsigned peers = __match_any_sync(0xffffffffu, valid ? dg : 0x10000u);
+    const unsigned peers = warp_digit_peers<RANK>(dg, valid);
     const unsigned before = __popc(peers & lt);
     const uint32_t prev = valid ? cnt[dg] : 0u;
     __syncwarp();

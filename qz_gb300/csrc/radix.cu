@@ -557,8 +557,13 @@ __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass0(Bi
     }
 }
 
-// One stable 8-bit pass (1..3) with decoupled look-back.
-template <int TILE>
+// One stable 8-bit pass (1..3) with decoupled look-back.  RANK: how a warp
+// finds the lanes with the same digit (warp_digit_peers).  EARLY: the tile's
+// digit counts come first, from shared-memory atomics, and are published
+// before the stable ranking, so that the tiles behind this one find them while
+// it ranks (otherwise the counts are published after the ranking, which
+// yields them as well).
+template <int TILE, int RANK, bool EARLY>
 __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass(
     BigArgs a, const uint32_t* __restrict__ h4, int pass, int w0, unsigned epoch, BigBuffers bb,
     unsigned long long* status, unsigned* ticket, DevStatus* st, unsigned spin_limit, int silent_tile) {
@@ -567,6 +572,7 @@ __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass(
     __shared__ int sval[TILE];
     __shared__ int vst[TILE];  // the tile's values in slot order (asynchronous copies)
     __shared__ uint32_t wcnt[kWarps][256];
+    __shared__ uint32_t tcnt[EARLY ? 256 : 1];  // the tile's digit counts (early publication)
     __shared__ uint32_t dig_off[256];
     __shared__ uint32_t gbase[256];
     __shared__ uint32_t sh[kWarps + 1];
@@ -591,6 +597,7 @@ __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass(
         }
 #pragma unroll
         for (int q = 0; q < kWarps; ++q) wcnt[q][threadIdx.x] = 0;
+        if (EARLY) tcnt[threadIdx.x] = 0;
         __syncthreads();
         int tau = s_tau;
         if (tau >= TT) return;
@@ -624,18 +631,34 @@ __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass(
         // are in flight; stored to shared memory only after the ranking, so
         // that the ranking starts as soon as the first keys arrive
         const uint32_t hb = h4[(size_t)s * kH4 + h4_row(pass) + threadIdx.x];
+        volatile unsigned long long* my = status + (size_t)tau * 256 + threadIdx.x;
+        const bool silent = j == silent_tile;  // failure-detection test only
+        if (EARLY) {
+            // counts only (no order): one shared atomic per slot
+#pragma unroll
+            for (int it = 0; it < IT; ++it) {
+                int i = (int)w * WSPAN + it * 32 + (int)ln;
+                if (i < cnt) atomicAdd(&tcnt[(kr[it] >> shift) & 255u], 1u);
+            }
+            __syncthreads();
+            const uint32_t c = tcnt[threadIdx.x];
+            if (j == 0)
+                *my = ep | kFlagInc | c;
+            else if (!silent)
+                *my = ep | kFlagAgg | c;
+        }
         // full tiles (all but a group's last) rank without per-slot
         // predicates.  The two loop bodies also keep the compiler from moving
         // key loads down into the ranking: measured 28.8 against 34.6 ms per
         // chunk forward on one lane, with long-scoreboard stalls halved.
         if (cnt == TILE) {
 #pragma unroll
-            for (int it = 0; it < IT; ++it) rk[it] = warp_digit_rank((kr[it] >> shift) & 255u, true, wcnt[w]);
+            for (int it = 0; it < IT; ++it) rk[it] = warp_digit_rank<RANK>((kr[it] >> shift) & 255u, true, wcnt[w]);
         } else {
 #pragma unroll
             for (int it = 0; it < IT; ++it) {
                 int i = (int)w * WSPAN + it * 32 + (int)ln;
-                rk[it] = warp_digit_rank((kr[it] >> shift) & 255u, i < cnt, wcnt[w]);
+                rk[it] = warp_digit_rank<RANK>((kr[it] >> shift) & 255u, i < cnt, wcnt[w]);
             }
         }
         gbase[threadIdx.x] = hb;
@@ -649,15 +672,13 @@ __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass(
                 wcnt[q][dg] = run;
                 run += c;
             }
-            // publish this tile's count, then find the counts of the tiles
-            // before it in the same group
-            volatile unsigned long long* my = status + (size_t)tau * 256 + dg;
+            // publish this tile's count (unless published early), then find
+            // the counts of the tiles before it in the same group
             uint32_t excl = 0;
-            const bool silent = j == silent_tile;  // failure-detection test only
             if (j == 0) {
-                *my = ep | kFlagInc | run;
+                if (!EARLY) *my = ep | kFlagInc | run;
             } else {
-                if (!silent) *my = ep | kFlagAgg | run;
+                if (!EARLY && !silent) *my = ep | kFlagAgg | run;
                 int p = tau - 1;
                 for (;;) {
                     volatile unsigned long long* q = status + (size_t)p * 256 + dg;
@@ -790,10 +811,22 @@ void big_sort_run(Storage* S, const BigArgs& a, const BigBuffers& bb, uint32_t* 
         unsigned* ticket = reinterpret_cast<unsigned*>(cnt + CNT_TICKET);
         if (!S->dry) cudaMemsetAsync(ticket, 0, sizeof(unsigned), st);
         const bool test = S->tune.lookback_test && pass == 1;
-        QZ_LAUNCH(S, st, "k_big_pass", 16 * elems,
-                  k_big_pass<TILE><<<pgrid, kThreads, 0, st>>>(a, h4, pass, w0, epoch, bb, f.status64, ticket,
-                                                               S->status, test ? 4096u : kSpinLimit,
-                                                               test ? 1 : -1));
+        const unsigned spin = test ? 4096u : kSpinLimit;
+        const int silent = test ? 1 : -1;
+#define QZ_BIG_PASS(R, E)                                                                                  \
+    QZ_LAUNCH(S, st, "k_big_pass", 16 * elems,                                                             \
+              (k_big_pass<TILE, R, E><<<pgrid, kThreads, 0, st>>>(a, h4, pass, w0, epoch, bb, f.status64, \
+                                                                  ticket, S->status, spin, silent)))
+        const bool early = S->tune.early_counts != 0;
+        switch (S->tune.rank_mode * 2 + (early ? 1 : 0)) {
+            case 2: QZ_BIG_PASS(1, false); break;
+            case 3: QZ_BIG_PASS(1, true); break;
+            case 4: QZ_BIG_PASS(2, false); break;
+            case 5: QZ_BIG_PASS(2, true); break;
+            case 1: QZ_BIG_PASS(0, true); break;
+            default: QZ_BIG_PASS(0, false); break;
+        }
+#undef QZ_BIG_PASS
     }
 }
 

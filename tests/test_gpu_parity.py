@@ -152,17 +152,19 @@ def test_decode_wrong_index_does_not_hang(gpu):
         assert e.code == native.QZGPU_DATA_CORRUPT
 
 
-@pytest.mark.parametrize("mode", [1, 2])
-def test_lookback_wait_runs_out_without_fault(gpu, oracle, mode):
+@pytest.mark.parametrize("mode,early", [(1, 0), (1, 1), (2, 0)])
+def test_lookback_wait_runs_out_without_fault(gpu, oracle, mode, early):
     # Failure detection: in the test mode one tile never publishes its
     # look-back status (mode 1: a tile of every large group in the radix sort;
     # mode 2: the second tile of every one-pass split), so the tiles
     # behind it give up after a short bounded wait; the call returns
     # QZGPU_TIMEOUT (no fault, no hang) and the same storage sorts correctly
-    # once the mode is off.
+    # once the mode is off.  `early`: the radix tiles publish their counts
+    # before their ranking.
     rng = np.random.default_rng(5)
     blocks = [rng.integers(0, 256, 1 << 20).astype(np.uint8)]  # one 2^20-slot group at the start
     with bwt.Storage(len(blocks[0]), 1) as st:
+        st.set_param("early_counts", early)
         st.set_param("split_lookback", 1 if mode == 2 else 0)
         st.set_param("lookback_test", mode)
         with pytest.raises(native.QzGpuError) as e:
@@ -179,12 +181,14 @@ def test_lookback_wait_runs_out_without_fault(gpu, oracle, mode):
 
 @pytest.mark.parametrize("params", [
     {"medium_max": 64, "big_ctas_per_sm": 2, "ruler_stride_log2": 3, "round_pipeline": 1},
-    {"split_lookback": 1},
-    {"split_lookback": 1, "round_pipeline": 1, "medium_max": 128},
-    {"medium_max": 512, "big_ctas_per_sm": 4, "fwd_sub_bytes": 1 << 20, "big_tile": 2048},
+    {"split_lookback": 1, "rank_mode": 1, "early_counts": 1},
+    {"split_lookback": 1, "round_pipeline": 1, "medium_max": 128, "rank_mode": 2},
+    {"medium_max": 512, "big_ctas_per_sm": 4, "fwd_sub_bytes": 1 << 20, "big_tile": 2048, "rank_mode": 1},
     {"medium_max": 128, "tile_ctas_per_sm": 1, "ruler_stride_log2": 7, "fwd_sub_bytes": 1 << 20,
      "inv_sub_bytes": 1 << 20, "big_tile": 8192, "radix_first_bits": 8, "round_pipeline": 1},
-    {"medium_max": 256, "big_ctas_per_sm": 1, "ruler_stride_log2": 4, "radix_first_bits": 9},
+    {"medium_max": 256, "big_ctas_per_sm": 1, "ruler_stride_log2": 4, "radix_first_bits": 9, "early_counts": 1},
+    {"rank_mode": 2, "early_counts": 1, "big_tile": 8192},
+    {"rank_mode": 0, "early_counts": 0, "medium_max": 64},
     {"ruler_stride_log2": 12, "round_pipeline": 1, "big_ctas_per_sm": 4},
 ])
 def test_tuned_knobs_keep_results(gpu, oracle, params):
