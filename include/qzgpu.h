@@ -165,6 +165,9 @@ int qzgpu_storage_round_counts(const qzgpu_storage *storage, long long *active, 
  *   "early_counts"                    stable radix pass: 1 (default) a tile publishes its
  *                                     digit counts for the look-back before it ranks,
  *                                     0 after
+ *   "pass0_bulk"                      radix pass 0: 1 (default) each CTA loads its next
+ *                                     tile by bulk copies while it sorts the current one,
+ *                                     0 one tile at a time by 4-byte asynchronous copies
  *   "lookback_test"                  failure-detection test: forward calls fail with
  *                                     QZGPU_TIMEOUT through a bounded look-back wait that
  *                                     runs out, no GPU fault (1: in the radix sort, 2: in

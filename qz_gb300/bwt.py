@@ -116,7 +116,7 @@ class Storage:
 
     PARAMS = ("fwd_sub_bytes", "inv_sub_bytes", "big_ctas_per_sm", "tile_ctas_per_sm", "medium_max",
               "ruler_stride_log2", "big_tile", "radix_first_bits", "round_pipeline", "split_lookback",
-              "rank_mode", "early_counts")
+              "rank_mode", "early_counts", "pass0_bulk")
 
     def set_param(self, name: str, value: int) -> None:
         check(self._lib.qzgpu_storage_set_param(self._h, name.encode(), int(value)), f"set_param({name})")

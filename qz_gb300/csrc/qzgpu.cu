@@ -692,6 +692,9 @@ int qzgpu_storage_set_param(qzgpu_storage* storage, const char* name, long long 
     } else if (k == "early_counts") {
         if (value < 0 || value > 1) return QZGPU_BAD_PARAMETER;
         each([&](Tune& t) { t.early_counts = (int)value; });
+    } else if (k == "pass0_bulk") {
+        if (value < 0 || value > 1) return QZGPU_BAD_PARAMETER;
+        each([&](Tune& t) { t.pass0_bulk = (int)value; });
     } else if (k == "lookback_test") {
         if (value < 0 || value > 2) return QZGPU_BAD_PARAMETER;
         each([&](Tune& t) { t.lookback_test = (int)value; });
@@ -717,6 +720,7 @@ long long qzgpu_storage_get_param(const qzgpu_storage* storage, const char* name
     if (k == "split_lookback") return t.split_lookback;
     if (k == "rank_mode") return t.rank_mode;
     if (k == "early_counts") return t.early_counts;
+    if (k == "pass0_bulk") return t.pass0_bulk;
     if (k == "lookback_test") return t.lookback_test;
     if (k == "lanes") return (long long)storage->lanes.size();
     return QZGPU_BAD_PARAMETER;

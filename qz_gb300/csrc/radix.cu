@@ -557,6 +557,179 @@ __global__ void __launch_bounds__(kThreads, big_min_ctas<TILE>()) k_big_pass0(Bi
     }
 }
 
+// Pass 0 with bulk copies, double-buffered.  A CTA's tiles are fixed (tau,
+// tau + grid, ...), so thread 0 issues the next tile's copies before the CTA
+// ranks and scatters the current one: the next tile's keys and values are in
+// flight during the whole of the current tile.  Each run is copied as its
+// 16-byte-aligned cover (one bulk copy for the keys, one for the values,
+// completed on the buffer's mbarrier; the arrays are 256-byte aligned and
+// followed by other arrays of the same allocation, so the cover stays inside
+// it) and indexed from its offset in the buffer.  Once a tile's keys and
+// values are in registers, its buffer doubles as the scatter staging.
+struct P0Desc {
+    int s, m;  // group, pass mask
+    int2 d;    // group's first slot and length
+    int j, wb; // tile within the group, workspace base
+    int n;     // slots in this tile
+    int ok, ov;  // element offsets of the keys and of the values in their buffers
+    int load;  // copies issued (the group runs pass 0)
+};
+
+template <int TILE>
+constexpr int p0_buf() { return TILE + 8; }  // a 4-byte run of TILE slots rounded out to 16 bytes
+template <int TILE>
+constexpr size_t p0_bulk_smem() { return sizeof(uint32_t) * (4 * (size_t)p0_buf<TILE>() + 2 * kH0); }
+template <int TILE>
+constexpr int p0_bulk_ctas() { return TILE >= 8192 ? 1 : (TILE <= 2048 ? 4 : 2); }
+constexpr unsigned kBulkSpinLimit = 1u << 22;  // mbarrier polls (each may suspend for a while)
+
+template <int TILE>
+__global__ void __launch_bounds__(kThreads, p0_bulk_ctas<TILE>()) k_big_pass0_bulk(BigArgs a,
+                                                                                 uint32_t* __restrict__ h4,
+                                                                                 BigBuffers bb, int w0,
+                                                                                 DevStatus* st) {
+    constexpr int IT = TILE / kThreads, WSPAN = TILE / kWarps, BUF = p0_buf<TILE>();
+    extern __shared__ __align__(128) uint32_t p0smem[];
+    uint32_t* kb = p0smem;                          // [2][BUF] keys
+    int* vb = reinterpret_cast<int*>(p0smem + 2 * BUF);  // [2][BUF] values
+    uint32_t* cnt = p0smem + 4 * BUF;               // [kH0] per-digit counts, then tile offsets
+    uint32_t* gb = cnt + kH0;                       // [kH0] group cursor minus tile offset
+    __shared__ uint32_t sh[kWarps + 1];
+    __shared__ __align__(8) unsigned long long bar[2];
+    __shared__ P0Desc sd[2];
+    const unsigned w = warp_id(), ln = lane_id();
+    const int nb0 = 1 << w0, per = nb0 / kThreads;
+    const uint32_t m0 = (uint32_t)nb0 - 1u;
+    const int TT = *a.ntiles;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    // thread 0: tile tau's descriptor (written out for the stable passes too)
+    // and, when its group runs pass 0, its copies into buffer bi
+    auto issue = [&](int tau, int bi) {
+        P0Desc D;
+        D.s = (int)a.tseg[tau];
+        D.m = (int)big_passes(a.gmask[D.s]);
+        D.d = a.list[D.s];
+        D.j = tau - (int)a.tbase[D.s];
+        D.wb = (int)a.wbase[D.s];
+        D.n = min(TILE, D.d.y - D.j * TILE);
+        a.tdesc[tau] = make_int4(D.s, D.m, D.d.x, D.wb);
+        a.tdesc2[tau] = make_int2(D.j, D.d.y);
+        D.load = D.m & 1;
+        D.ok = D.ov = 0;
+        if (D.load) {
+            const BigRoute rt = big_route(bb, D.d, (uint32_t)D.wb, (uint32_t)D.m, 0);
+            const uint32_t* ks = rt.sk + (size_t)D.j * TILE;
+            const int* vs = rt.sv + (size_t)D.j * TILE;
+            D.ok = (int)(((uintptr_t)ks & 15u) >> 2);
+            D.ov = (int)(((uintptr_t)vs & 15u) >> 2);
+            const unsigned kbytes = ((unsigned)(D.ok + D.n) * 4u + 15u) & ~15u;
+            const unsigned vbytes = ((unsigned)(D.ov + D.n) * 4u + 15u) & ~15u;
+            fence_proxy_async_smem();  // the buffer's last reads and writes come first
+            mbar_arrive_expect_tx(&bar[bi], kbytes + vbytes);
+            bulk_g2s(kb + bi * BUF, reinterpret_cast<const void*>((uintptr_t)ks & ~(uintptr_t)15), kbytes, &bar[bi]);
+            bulk_g2s(vb + bi * BUF, reinterpret_cast<const void*>((uintptr_t)vs & ~(uintptr_t)15), vbytes, &bar[bi]);
+        }
+        sd[bi] = D;
+    };
+    if (threadIdx.x == 0 && (int)blockIdx.x < TT) issue((int)blockIdx.x, 0);
+    unsigned par = 0;  // bit bi: parity of buffer bi's next phase
+    int b = 0;
+    for (int tau = blockIdx.x; tau < TT; tau += gridDim.x, b ^= 1) {
+        if (threadIdx.x == 0 && tau + (int)gridDim.x < TT) issue(tau + (int)gridDim.x, b ^ 1);
+        for (int i = threadIdx.x; i < nb0; i += kThreads) cnt[i] = 0;
+        __syncthreads();  // sd[b] (issued one tile earlier) and the cleared counts
+        const P0Desc D = sd[b];
+        if (!D.load) {
+            __syncthreads();  // everyone has read sd[b] before it is issued again
+            continue;
+        }
+        bool ok = mbar_wait(&bar[b], par >> b & 1u, kBulkSpinLimit);
+        par ^= 1u << b;
+        if (!ok) {
+            // copies that never completed: record it, give them a second
+            // bounded wait (they write this buffer) and store nothing
+            if (threadIdx.x == 0) report(st, QZGPU_TIMEOUT, 22, tau);
+            mbar_wait(&bar[b], (par >> b & 1u) ^ 1u, kBulkSpinLimit);
+        }
+        if (!__syncthreads_and(ok)) {
+            __syncthreads();
+            continue;
+        }
+        const BigRoute rt = big_route(bb, D.d, (uint32_t)D.wb, (uint32_t)D.m, 0);
+        uint32_t* dk = rt.dk;
+        int* dv = rt.dv;
+        const int n = D.n;
+        uint32_t* kc = kb + b * BUF;
+        int* vc = vb + b * BUF;
+        uint32_t kr[IT], rk[IT];
+        int vr[IT];
+        if (n == TILE) {
+#pragma unroll
+            for (int it = 0; it < IT; ++it) {
+                const int i = (int)w * WSPAN + it * 32 + (int)ln;
+                kr[it] = kc[D.ok + i];
+                vr[it] = vc[D.ov + i];
+            }
+#pragma unroll
+            for (int it = 0; it < IT; ++it) rk[it] = atomicAdd(&cnt[kr[it] & m0], 1u);
+        } else {
+#pragma unroll
+            for (int it = 0; it < IT; ++it) {
+                const int i = (int)w * WSPAN + it * 32 + (int)ln;
+                kr[it] = i < n ? kc[D.ok + i] : 0u;
+                vr[it] = i < n ? vc[D.ov + i] : 0;
+                rk[it] = i < n ? atomicAdd(&cnt[kr[it] & m0], 1u) : 0u;
+            }
+        }
+        __syncthreads();
+        {
+            uint32_t c[kH0 / kThreads];
+            uint32_t sum = 0;
+#pragma unroll
+            for (int i = 0; i < kH0 / kThreads; ++i) {
+                c[i] = i < per ? cnt[threadIdx.x * per + i] : 0u;
+                sum += c[i];
+            }
+            uint32_t tot;
+            uint32_t off = block_excl_sum(sum, sh, &tot);
+#pragma unroll
+            for (int i = 0; i < kH0 / kThreads; ++i) {
+                if (i < per) {
+                    const int dg = threadIdx.x * per + i;
+                    const uint32_t base = c[i] ? atomicAdd(&h4[(size_t)D.s * kH4 + dg], c[i]) : 0u;
+                    cnt[dg] = off;
+                    gb[dg] = base - off;
+                    off += c[i];
+                }
+            }
+        }
+        __syncthreads();
+        // the buffer's contents are in registers: stage the scatter there
+#pragma unroll
+        for (int it = 0; it < IT; ++it) {
+            const int i = (int)w * WSPAN + it * 32 + (int)ln;
+            if (i < n) {
+                const uint32_t lp = cnt[kr[it] & m0] + rk[it];
+                kc[lp] = kr[it];
+                vc[lp] = vr[it];
+            }
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += kThreads) {
+            const uint32_t kv = kc[i];
+            const uint32_t dst = gb[kv & m0] + (uint32_t)i;
+            dk[dst] = kv;
+            dv[dst] = vc[i];
+        }
+        __syncthreads();  // the buffer and sd[b] are free for the tile after next
+    }
+}
+
 // One stable 8-bit pass (1..3) with decoupled look-back.  RANK: how a warp
 // finds the lanes with the same digit (warp_digit_peers).  EARLY: the tile's
 // digit counts come first, from shared-memory atomics, and are published
@@ -800,7 +973,19 @@ void big_sort_run(Storage* S, const BigArgs& a, const BigBuffers& bb, uint32_t* 
               k_big_bases<<<grid_cap(4ll * host_count, 1, sms * 8), kThreads, 0, st>>>(a, h4, w0));
     // pass 0: unstable, no look-back (bytes are an upper bound: passes whose
     // digit is constant in a group are skipped for that group)
-    QZ_LAUNCH(S, st, "k_big_pass0", 16 * elems, k_big_pass0<TILE><<<grid, kThreads, 0, st>>>(a, h4, bb, w0));
+    if (S->tune.pass0_bulk) {
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(k_big_pass0_bulk<TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)p0_bulk_smem<TILE>());
+            attr = true;
+        }
+        QZ_LAUNCH(S, st, "k_big_pass0", 16 * elems,
+                  k_big_pass0_bulk<TILE><<<sms * p0_bulk_ctas<TILE>(), kThreads, p0_bulk_smem<TILE>(), st>>>(
+                      a, h4, bb, w0, S->status));
+    } else {
+        QZ_LAUNCH(S, st, "k_big_pass0", 16 * elems, k_big_pass0<TILE><<<grid, kThreads, 0, st>>>(a, h4, bb, w0));
+    }
     // stable passes: decoupled look-back over a persistent grid, tiles taken
     // by ticket (a tile waits only on tiles of earlier tickets, whose CTAs are
     // resident, so the grid may exceed what fits at once)

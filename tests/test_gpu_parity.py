@@ -187,8 +187,10 @@ def test_lookback_wait_runs_out_without_fault(gpu, oracle, mode, early):
     {"medium_max": 128, "tile_ctas_per_sm": 1, "ruler_stride_log2": 7, "fwd_sub_bytes": 1 << 20,
      "inv_sub_bytes": 1 << 20, "big_tile": 8192, "radix_first_bits": 8, "round_pipeline": 1},
     {"medium_max": 256, "big_ctas_per_sm": 1, "ruler_stride_log2": 4, "radix_first_bits": 9, "early_counts": 1},
-    {"rank_mode": 2, "early_counts": 1, "big_tile": 8192},
-    {"rank_mode": 0, "early_counts": 0, "medium_max": 64},
+    {"rank_mode": 2, "early_counts": 1, "big_tile": 8192, "pass0_bulk": 0},
+    {"rank_mode": 0, "early_counts": 0, "medium_max": 64, "pass0_bulk": 0},
+    {"pass0_bulk": 1, "big_tile": 2048, "radix_first_bits": 8},
+    {"pass0_bulk": 1, "fwd_sub_bytes": 1 << 20, "round_pipeline": 1},
     {"ruler_stride_log2": 12, "round_pipeline": 1, "big_ctas_per_sm": 4},
 ])
 def test_tuned_knobs_keep_results(gpu, oracle, params):
