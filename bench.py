@@ -600,20 +600,28 @@ def run_gpu(args, rank: int, world: int):
             h[:] = b
         h_u = [pinned(len(b)) for b in blocks]
         h_back = [pinned(len(b)) for b in blocks]
-        us, ix = st.encode_batch(h_in, out=h_u)
-        st.decode_batch(h_u, ix, out=h_back)
+        for _ in range(2):
+            us, ix = st.encode_batch(h_in, out=h_u)
+            st.decode_batch(h_u, ix, out=h_back)
         if dist:
             dist.barrier()
+        fwd_s = inv_s = 0.0
         t0 = time.perf_counter()
         for _ in range(args.steps):
+            ta = time.perf_counter()
             us, ix = st.encode_batch(h_in, out=h_u)
+            tb = time.perf_counter()
             back = st.decode_batch(h_u, ix, out=h_back)
+            fwd_s += tb - ta
+            inv_s += time.perf_counter() - tb
         t1 = time.perf_counter()
         if not all(np.array_equal(a, b) for a, b in zip(back, blocks)):
             raise SystemExit("host round trip mismatch")
-        e2e_s = max_over_ranks([t1 - t0], dist)[0]
+        e2e_s, fwd_s, inv_s = max_over_ranks([t1 - t0, fwd_s, inv_s], dist)
         e2e = {"value": round(job_rate(world, N, args.steps, e2e_s), 3), "unit": "MB/s",
                "h2d_bytes_per_step": 2 * N, "d2h_bytes_per_step": 2 * N,
+               "fwd_ms_per_step": round(fwd_s / args.steps * 1e3, 3),
+               "inv_ms_per_step": round(inv_s / args.steps * 1e3, 3),
                "api": "qzgpu_bwt_encode_batch + qzgpu_bwt_decode_batch (pinned host buffers, reused)"}
     st.close()
 

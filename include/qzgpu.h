@@ -162,9 +162,9 @@ int qzgpu_storage_round_counts(const qzgpu_storage *storage, long long *active, 
  *   "rank_mode"                       how a stable radix pass ranks a warp's digits:
  *                                     0 warp match, 1 eight ballots, 2 a match on the
  *                                     high four bits and four ballots (default)
- *   "early_counts"                    stable radix pass: 1 (default) a tile publishes its
- *                                     digit counts for the look-back before it ranks,
- *                                     0 after
+ *   "early_counts"                    stable radix pass: 1 a tile publishes its digit
+ *                                     counts for the look-back before it ranks, 0 after
+ *                                     (default)
  *   "pass0_bulk"                      radix pass 0: 1 (default) each CTA loads its next
  *                                     tile by bulk copies while it sorts the current one,
  *                                     0 one tile at a time by 4-byte asynchronous copies

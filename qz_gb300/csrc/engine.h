@@ -102,7 +102,7 @@ struct Tune {
     int round_pipeline = 0;    // forward rounds: 0 issued after the host reads their counts, 1 issued ahead
     int split_lookback = 0;    // split: 0 count + scan + apply passes, 1 one pass with decoupled look-back
     int rank_mode = 2;         // stable radix pass digit ranking: 0 warp match, 1 ballots, 2 match + ballots
-    int early_counts = 1;      // stable radix pass: 1 digit counts published before the ranking
+    int early_counts = 0;      // stable radix pass: 1 digit counts published before the ranking
     int pass0_bulk = 1;        // radix pass 0: 1 double-buffered bulk copies of the next tile
     // failure-detection test: 1: in the first stable radix pass the second
     // tile of every group publishes nothing; 2: in every one-pass split the
