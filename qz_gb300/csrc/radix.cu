@@ -36,6 +36,7 @@ constexpr int kOItems = kOT / kThreads;   // 16 slots per thread
 constexpr unsigned long long kFlagAgg = 1ull << 32;
 constexpr unsigned long long kFlagInc = 2ull << 32;
 constexpr unsigned kSpinLimit = 1u << 24;
+constexpr unsigned kBulkSpinLimit = 1u << 22;  // mbarrier polls for a bulk copy (each may suspend for a while)
 
 // Pass-0 bins at most (an 11-bit first digit) and digit-count words per
 // listed group of the large-group sort (pass 0's bins, then 256 per later pass).
@@ -581,7 +582,6 @@ template <int TILE>
 constexpr size_t p0_bulk_smem() { return sizeof(uint32_t) * (4 * (size_t)p0_buf<TILE>() + 2 * kH0); }
 template <int TILE>
 constexpr int p0_bulk_ctas() { return TILE >= 8192 ? 1 : (TILE <= 2048 ? 4 : 2); }
-constexpr unsigned kBulkSpinLimit = 1u << 22;  // mbarrier polls (each may suspend for a while)
 
 template <int TILE>
 __global__ void __launch_bounds__(kThreads, p0_bulk_ctas<TILE>()) k_big_pass0_bulk(BigArgs a,
