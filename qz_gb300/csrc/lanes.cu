@@ -24,6 +24,22 @@ namespace {
 
 constexpr long long kTouchMinBytes = 8ll << 20;  // smaller host batches copy out directly
 
+// True when every output buffer is page-locked host memory (cudaMallocHost,
+// cudaHostAlloc or cudaHostRegister): its pages are resident, so copies into
+// it need no touching first.
+bool outputs_pinned(int nb, const int* n, unsigned char* const* hout) {
+    for (int b = 0; b < nb; ++b) {
+        if (n[b] <= 0) continue;
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, hout[b]) != cudaSuccess) {
+            cudaGetLastError();  // clear it: the pointer is plain pageable memory
+            return false;
+        }
+        if (at.type != cudaMemoryTypeHost) return false;
+    }
+    return true;
+}
+
 int lanes_for(long long cap_bytes) {
     const char* env = getenv("QZGPU_LANES");
     if (env && atoi(env) > 0) return std::min(atoi(env), 16);
@@ -120,13 +136,14 @@ int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned cha
     // times slower than into resident pages.  A host thread touches one byte
     // per page of every output buffer, sub-batch by sub-batch in the order the
     // lanes take them, while the device works; a lane waits for its
-    // sub-batch's pages before it copies the blocks out.
+    // sub-batch's pages before it copies the blocks out.  Page-locked outputs
+    // are resident already and are not touched.
     const int nsub = (int)order.size();
     std::atomic<int> touched{nsub};  // sub-batches (in `order`) whose pages are touched
     std::mutex tmu;
     std::condition_variable tcv;
     std::thread toucher;
-    if (host && off >= kTouchMinBytes) {
+    if (host && off >= kTouchMinBytes && !outputs_pinned(nb, n, hout)) {
         touched = 0;
         toucher = std::thread([&] {
             for (int k = 0; k < nsub; ++k) {

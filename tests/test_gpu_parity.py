@@ -243,6 +243,27 @@ def test_batch_fresh_outputs_above_touch_threshold(gpu, oracle):
         assert all((x == y).all() for x, y in zip(back, blocks))
 
 
+@pytest.mark.parametrize("pinned", ["all", "some"])
+def test_batch_pinned_outputs_above_touch_threshold(gpu, oracle, pinned):
+    # page-locked outputs are resident: the engine skips touching them (all
+    # pinned); one pageable output among them brings the touching back
+    import torch
+    blocks = _big_blocks()
+
+    def out(n, i):
+        if pinned == "some" and i == 1:
+            return np.empty(n, np.uint8)
+        return torch.empty(n, dtype=torch.uint8, pin_memory=True).numpy()
+
+    with bwt.Storage(sum(len(b) for b in blocks), len(blocks)) as st:
+        us, idx = st.encode_batch(blocks, out=[out(len(b), i) for i, b in enumerate(blocks)])
+        ous, oidx = oracle.bwt_encode_batch(blocks)
+        assert idx == list(oidx)
+        assert all((u == ou).all() for u, ou in zip(us, ous))
+        back = st.decode_batch(us, idx, out=[out(len(b), i) for i, b in enumerate(blocks)])
+        assert all((x == y).all() for x, y in zip(back, blocks))
+
+
 def test_batch_in_place_above_touch_threshold(gpu, oracle):
     import ctypes
     blocks = _big_blocks()
