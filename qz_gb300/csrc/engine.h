@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <condition_variable>
 #include <cstring>
 #include <functional>
@@ -276,6 +277,18 @@ void dump_array(const char* name, const void* dptr, size_t bytes, cudaStream_t s
 cudaEvent_t prof_begin(Storage* S, cudaStream_t st, const char* name);
 void prof_end(Storage* S, cudaStream_t st, const char* name, long long bytes, cudaEvent_t a);
 void prof_flush(Storage* S);  // after the stream is idle: fold pending records in
+// Raises kernel K's dynamic shared memory limit to `bytes` on the current
+// device, once per device (the attribute belongs to the device; one bit per
+// device number below 64, later devices set it at every launch).
+template <auto K>
+inline void smem_limit_once(int bytes, int device) {
+    static std::atomic<unsigned long long> done{0};
+    const unsigned long long bit = device >= 0 && device < 64 ? 1ull << device : 0ull;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) return;
+    cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    done.fetch_or(bit, std::memory_order_acq_rel);
+}
+
 // Launch wrapper: counts the launch, times it when profiling, checks it in debug mode.
 #define QZ_LAUNCH(S, st, name, bytes, ...)                     \
     do {                                                       \

@@ -1201,11 +1201,7 @@ void sort_rbc_groups(Storage* S, const int2* list, const int* d_count, int host_
 void sort_medium_groups(Storage* S, const int2* list, const int* d_count, int host_count, long long elems,
                         const uint32_t* skey, const int* sval, uint32_t* key, int* val, cudaStream_t st) {
     if (host_count <= 0) return;
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_sort_medium, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kWarps * kMedWarpSmem));
-        attr = true;
-    }
+    smem_limit_once<k_sort_medium>((int)(kWarps * kMedWarpSmem), S->device);
     QZ_LAUNCH(S, st, "k_sort_medium", 16 * elems + 8ll * host_count,
               k_sort_medium<<<grid_for(host_count, kWarps, S->sms * 16), kThreads, kWarps * kMedWarpSmem, st>>>(
                   list, d_count, skey, sval, key, val));

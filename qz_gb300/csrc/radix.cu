@@ -932,11 +932,7 @@ void sort_tile_groups(Storage* S, const int2* list, const int* d_count, int host
                       cudaStream_t st) {
     if (host_count <= 0) return;
     const int w0 = first_digit_bits(key_bits, S->tune.first_digit_max);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_tile_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_sort_smem());
-        attr = true;
-    }
+    smem_limit_once<k_tile_sort>((int)tile_sort_smem(), S->device);
     QZ_LAUNCH(S, st, "k_tile_sort", 16 * elems,
               k_tile_sort<<<grid_cap(host_count, 1, S->sms * S->tune.tile_ctas_per_sm), kThreads, tile_sort_smem(),
                             st>>>(list, d_count, skey, sval, key, val, w0));
@@ -974,12 +970,7 @@ void big_sort_run(Storage* S, const BigArgs& a, const BigBuffers& bb, uint32_t* 
     // pass 0: unstable, no look-back (bytes are an upper bound: passes whose
     // digit is constant in a group are skipped for that group)
     if (S->tune.pass0_bulk) {
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(k_big_pass0_bulk<TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)p0_bulk_smem<TILE>());
-            attr = true;
-        }
+        smem_limit_once<k_big_pass0_bulk<TILE>>((int)p0_bulk_smem<TILE>(), S->device);
         QZ_LAUNCH(S, st, "k_big_pass0", 16 * elems,
                   k_big_pass0_bulk<TILE><<<sms * p0_bulk_ctas<TILE>(), kThreads, p0_bulk_smem<TILE>(), st>>>(
                       a, h4, bb, w0, S->status));
