@@ -154,8 +154,15 @@ struct Storage {
     char* pin = nullptr;
     size_t pin_bytes = 0;
     char* pin_tab = nullptr;   // tables
+    char* pin_tab_alt = nullptr;  // second table area (chained inverse sub-batches alternate)
     int* pin_rd = nullptr;     // small device->host readbacks
     size_t pin_tab_bytes = 0;
+    // chained inverse sub-batches: the table area the next one fills, the
+    // event after each area's last table copies, and work issued but not yet
+    // checked
+    int tab_slot = 0;
+    cudaEvent_t tab_ev[2] = {nullptr, nullptr};
+    bool inv_chained = false;
 
     std::mutex mu;
     qzgpu_stats stats{};
@@ -247,6 +254,15 @@ int forward_run(Storage* S, int nb, const int* n, const uint8_t* d_T, uint8_t* d
 // inverted correctly, the others could not be inverted.
 int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t* d_U, uint8_t* d_T,
                 cudaStream_t st, int* block_rc = nullptr);
+// The same, issued without waiting for it (chained = true): the call returns
+// once the work is queued on st.  Tables alternate between two pinned areas;
+// the device status is neither cleared nor read, so a chain starts with
+// inverse_chain_begin and ends with inverse_chain_end, which waits for the
+// stream and returns the first failure of any link.
+int inverse_run_chained(Storage* S, int nb, const int* n, const int* idx, const uint8_t* d_U, uint8_t* d_T,
+                        cudaStream_t st);
+void inverse_chain_begin(Storage* S, cudaStream_t st);
+int inverse_chain_end(Storage* S, cudaStream_t st);
 
 int map_cuda_error(cudaError_t e);
 // The library's device (initialised on first use) and its SM count.
@@ -264,6 +280,12 @@ int encode_host(Storage* S, int nb, const unsigned char* const* T, unsigned char
 // given, a call that fails only for some blocks still copies every block out.
 int decode_host(Storage* S, int nb, const unsigned char* const* U, unsigned char* const* T, const int* n,
                 const int* idx, const std::function<void()>* before_copy_out = nullptr, int* block_rc = nullptr);
+// A link of a chain of host-buffer inverse sub-batches on one storage (copies
+// in, inverse, copies out, all queued on the storage's stream without a wait;
+// see inverse_run_chained).  The caller's buffers must stay valid until
+// inverse_chain_end.
+int decode_host_chained(Storage* S, int nb, const unsigned char* const* U, unsigned char* const* T, const int* n,
+                        const int* idx, const std::function<void()>* before_copy_out);
 
 // Debug mode (environment QZGPU_DEBUG=1): every launch is followed by a
 // stream synchronize and an error check, and failures are logged to stderr.

@@ -465,8 +465,13 @@ size_t inverse_stage_bytes(long long cap_bytes, int cap_blocks) {
     return 4 * (size_t)cap_bytes + (size_t)stage_cap(12) * (size_t)(cap_blocks + 1);
 }
 
-int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t* d_U, uint8_t* d_T,
-                cudaStream_t st, int* block_rc) {
+namespace {
+
+// The inverse of one batch.  chained: tables go to the area the chain fills
+// next (after that area's previous copies have run), the device status is
+// left to the chain, and the call returns once the work is queued.
+int inverse_issue(Storage* S, int nb, const int* n, const int* idx, const uint8_t* d_U, uint8_t* d_T,
+                  cudaStream_t st, int* block_rc, bool chained) {
     if (nb < 0 || nb > S->cap_blocks) return QZGPU_BAD_PARAMETER;
     long long N = 0;
     for (int b = 0; b < nb; ++b) {
@@ -508,7 +513,13 @@ int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t*
     if ((size_t)tbase[nb] * 256 > S->hist_cap) return QZGPU_BAD_PARAMETER;
     size_t need = sizeof(int) * (5 * (nb + 1)) + sizeof(int2) * (tiles.size() + rtiles.size()) + 256;
     if (need > S->pin_tab_bytes) return QZGPU_BAD_PARAMETER;
-    char* p = S->pin_tab;
+    const int slot = S->tab_slot;
+    if (chained) {
+        // the copies that last read this area must have run before it is refilled
+        const cudaError_t w = cudaEventSynchronize(S->tab_ev[slot]);
+        if (w != cudaSuccess) return map_cuda_error(w);
+    }
+    char* p = chained && slot ? S->pin_tab_alt : S->pin_tab;
     auto put = [&](const void* src, size_t bytes) {
         char* at = p;
         if (bytes) memcpy(p, src, bytes);
@@ -534,7 +545,11 @@ int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t*
     h2d(S->blk_hbase, h_hb, sizeof(int) * hbase.size());
     h2d(S->tiles, h_tiles, sizeof(int2) * tiles.size());
     h2d(v.rtiles, h_rt, sizeof(int2) * rtiles.size());
-    if (e == cudaSuccess) e = cudaMemsetAsync(S->status, 0, sizeof(DevStatus), st);
+    if (chained && e == cudaSuccess) {
+        e = cudaEventRecord(S->tab_ev[slot], st);
+        S->tab_slot = slot ^ 1;
+    }
+    if (!chained && e == cudaSuccess) e = cudaMemsetAsync(S->status, 0, sizeof(DevStatus), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(S->blk_status, 0, sizeof(int) * nb, st);
     // a ruler no head reaches (corrupt input) keeps -1 and is reported
     if (e == cudaSuccess) e = cudaMemsetAsync(v.distF, 0xff, sizeof(int) * Mtot, st);
@@ -571,6 +586,11 @@ int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t*
               k_inv_place<<<pgrid, kThreads, 0, st>>>(a, r, nb, Mtot, d_T));
     // walks longer than the staging slot: their tails only
     QZ_LAUNCH(S, st, "k_inv_walk2", 12ll * Mtot, k_inv_walk2<<<nrt, kThreads, 0, st>>>(a, r, S->hist, d_T));
+    if (chained) {
+        S->stats.kernel_launches = S->launches;
+        S->stats.alg_bytes = 12 * N;
+        return map_cuda_error(cudaGetLastError());
+    }
     DevStatus* hst = reinterpret_cast<DevStatus*>(S->pin_rd);
     int* hbs = S->pin_rd + 64;  // per-block results (pinned; nb <= cap_blocks entries fit)
     e = cudaMemcpyAsync(hst, S->status, sizeof(DevStatus), cudaMemcpyDeviceToHost, st);
@@ -596,6 +616,36 @@ int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t*
     S->stats.kernel_launches = S->launches;
     S->stats.alg_bytes = 12 * N;
     return QZGPU_NO_ERROR;
+}
+
+}  // namespace
+
+int inverse_run(Storage* S, int nb, const int* n, const int* idx, const uint8_t* d_U, uint8_t* d_T,
+                cudaStream_t st, int* block_rc) {
+    return inverse_issue(S, nb, n, idx, d_U, d_T, st, block_rc, false);
+}
+
+int inverse_run_chained(Storage* S, int nb, const int* n, const int* idx, const uint8_t* d_U, uint8_t* d_T,
+                        cudaStream_t st) {
+    return inverse_issue(S, nb, n, idx, d_U, d_T, st, nullptr, true);
+}
+
+void inverse_chain_begin(Storage* S, cudaStream_t st) {
+    cudaMemsetAsync(S->status, 0, sizeof(DevStatus), st);
+    S->inv_chained = true;
+}
+
+int inverse_chain_end(Storage* S, cudaStream_t st) {
+    S->inv_chained = false;
+    DevStatus* hst = reinterpret_cast<DevStatus*>(S->pin_rd);
+    cudaError_t e = cudaMemcpyAsync(hst, S->status, sizeof(DevStatus), cudaMemcpyDeviceToHost, st);
+    const cudaError_t w = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = w;
+    if (e != cudaSuccess) return map_cuda_error(e);
+    prof_flush(S);
+    if (hst->error && debug_on())
+        debug_log("device status %d at %d detail %lld", hst->error, hst->where, hst->detail);
+    return hst->error;
 }
 
 }  // namespace qz

@@ -180,9 +180,16 @@ int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned cha
                 std::unique_lock<std::mutex> lk(tmu);
                 tcv.wait(lk, [&] { return touched.load() > sb.seq; });
             };
-            rc = forward ? encode_host(S, cnt, hin + sb.b0, hout + sb.b0, n + sb.b0, idx + sb.b0, nullptr, nullptr,
-                                       &wait_out)
-                         : decode_host(S, cnt, hin + sb.b0, hout + sb.b0, n + sb.b0, idx + sb.b0, &wait_out);
+            if (forward) {
+                rc = encode_host(S, cnt, hin + sb.b0, hout + sb.b0, n + sb.b0, idx + sb.b0, nullptr, nullptr,
+                                 &wait_out);
+            } else {
+                // a lane's inverse sub-batches are queued back to back on its
+                // stream (copies in, inverse, copies out) and checked once at
+                // the end, so no lane waits for the device between them
+                if (!S->inv_chained) inverse_chain_begin(S, S->stream);
+                rc = decode_host_chained(S, cnt, hin + sb.b0, hout + sb.b0, n + sb.b0, idx + sb.b0, &wait_out);
+            }
         } else {
             rc = forward ? forward_run(S, cnt, n + sb.b0, d_in + sb.off, d_out + sb.off, idx + sb.b0, nullptr,
                                        nullptr, S->stream)
@@ -211,6 +218,12 @@ int engine_run(Engine* E, bool forward, int nb, const int* n, const unsigned cha
                 int i = cursor.fetch_add(1);
                 if (i >= (int)small.size() || first_err.load()) break;
                 run_sub(lane, small[i]);
+            }
+            Storage* S = E->lanes[lane].get();
+            if (S->inv_chained) {
+                const int rc = inverse_chain_end(S, S->stream);
+                int z = 0;
+                if (rc) first_err.compare_exchange_strong(z, rc);
             }
         };
         E->job_done = 0;

@@ -353,9 +353,9 @@ int storage_init(Storage* S, long long cap_bytes, int cap_blocks) {
     }
     S->dev_bytes = bytes;
     layout(S, S->dev, c);
-    S->pin_tab_bytes = pinned_table_bytes(c);
+    S->pin_tab_bytes = (pinned_table_bytes(c) + 255) / 256 * 256;
     size_t rd = sizeof(int) * (c.nb + 256);
-    S->pin_bytes = S->pin_tab_bytes + rd + 64;
+    S->pin_bytes = 2 * S->pin_tab_bytes + rd + 64;
     e = cudaMallocHost(&S->pin, S->pin_bytes);
     if (e != cudaSuccess) {
         cudaFree(S->dev);
@@ -364,9 +364,11 @@ int storage_init(Storage* S, long long cap_bytes, int cap_blocks) {
         return QZGPU_NOT_ENOUGH_MEMORY;
     }
     S->pin_tab = S->pin;
-    S->pin_rd = reinterpret_cast<int*>(S->pin_tab + S->pin_tab_bytes);
+    S->pin_tab_alt = S->pin + S->pin_tab_bytes;
+    S->pin_rd = reinterpret_cast<int*>(S->pin_tab_alt + S->pin_tab_bytes);
     e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking);
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&S->round_ev[i], cudaEventDisableTiming);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&S->tab_ev[i], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         storage_free(S);
         return map_cuda_error(e);
@@ -378,6 +380,10 @@ void storage_free(Storage* S) {
     for (auto e : S->ev_pool) cudaEventDestroy(e);
     S->ev_pool.clear();
     for (auto& e : S->round_ev) {
+        if (e) cudaEventDestroy(e);
+        e = nullptr;
+    }
+    for (auto& e : S->tab_ev) {
         if (e) cudaEventDestroy(e);
         e = nullptr;
     }
@@ -462,6 +468,32 @@ int decode_host(Storage* S, int nb, const unsigned char* const* U, unsigned char
     }
     e = cudaStreamSynchronize(S->stream);
     return e != cudaSuccess ? map_cuda_error(e) : rc;
+}
+
+int decode_host_chained(Storage* S, int nb, const unsigned char* const* U, unsigned char* const* T, const int* n,
+                        const int* idx, const std::function<void()>* before_copy_out) {
+    cudaError_t e = cudaSetDevice(S->device);
+    if (e != cudaSuccess) return map_cuda_error(e);
+    long long off = 0;
+    for (int b = 0; b < nb; ++b) {
+        if (n[b] > 0) {
+            e = cudaMemcpyAsync(S->U + off, U[b], (size_t)n[b], cudaMemcpyHostToDevice, S->stream);
+            if (e != cudaSuccess) return map_cuda_error(e);
+        }
+        off += n[b];
+    }
+    const int rc = inverse_run_chained(S, nb, n, idx, S->U, S->T, S->stream);
+    if (rc) return rc;
+    if (before_copy_out) (*before_copy_out)();
+    off = 0;
+    for (int b = 0; b < nb; ++b) {
+        if (n[b] > 0) {
+            e = cudaMemcpyAsync(T[b], S->T + off, (size_t)n[b], cudaMemcpyDeviceToHost, S->stream);
+            if (e != cudaSuccess) return map_cuda_error(e);
+        }
+        off += n[b];
+    }
+    return QZGPU_NO_ERROR;
 }
 
 int device_info(int* device, int* sms) {
