@@ -113,3 +113,16 @@ def test_sais_agrees_with_doubling_at_megabytes(oracle, kind):
     u, idx = oracle.bwt_encode(t)
     assert (oracle.bwt_decode(u, idx) == t).all()
 
+
+
+def test_tuned_build_keeps_the_base_instruction_set():
+    # The timed CPU baseline loads the tuned oracle on the GPU hosts, whose
+    # kernels expose no SVE to user space: the aarch64 build may tune for the
+    # core but must not select an instruction set beyond the base one (an
+    # -mcpu=neoverse-v2 build emitted SVE and stopped with SIGILL there).
+    mk = open(os.path.join(os.path.dirname(__file__), "..", "oracle", "Makefile")).read()
+    arm = mk.split("ifeq ($(ARCH),aarch64)", 1)[1].split("else", 1)[0]
+    tune = [ln.split(":=", 1)[1].split() for ln in arm.splitlines() if ln.strip().startswith("TUNE")]
+    assert tune and all(f.startswith("-mtune=") for f in tune[0]), tune
+    assert "-mcpu" not in mk.split("TUNED_CFLAGS", 1)[1].split("\n", 1)[0]
+    assert "native" not in mk.split("TUNED_CFLAGS", 1)[1].split("\n", 1)[0]
