@@ -77,3 +77,34 @@ def test_noalloc_in_place_and_large_then_small():
         torch.cuda.synchronize()
         assert np.array_equal(d.cpu().numpy(), expected)
         assert np.array_equal(expected, t)
+
+
+def test_noalloc_one_byte_and_wrong_index():
+    # a 1-byte block is its own transform; a wrong but in-range index gives
+    # the existing entry point's answer (the same bytes, or the same
+    # corrupt-data error), and the call returns either way
+    torch = pytest.importorskip("torch")
+    lib = native.load()
+    bwt.init()
+    stream = torch.cuda.current_stream().cuda_stream
+    one = torch.tensor([0x41], dtype=torch.uint8, device="cuda")
+    out = torch.zeros_like(one)
+    rc = _noalloc(lib, one.data_ptr(), out.data_ptr(), 1, 1, stream)
+    assert rc == native.QZGPU_NO_ERROR, native.error_string(rc)
+    torch.cuda.synchronize()
+    assert out.cpu().numpy().tolist() == [0x41]
+
+    t = synth.sample_reads(synth.uniform_genome(5000, seed=53), 50, seed=54)
+    u, idx = bwt.bwt_encode(t)
+    wrong = idx % len(t) + 1
+    try:
+        expected, want_rc = bwt.bwt_decode(u, wrong), native.QZGPU_NO_ERROR
+    except native.QzGpuError as e:
+        expected, want_rc = None, e.code
+    d_u = torch.from_numpy(np.ascontiguousarray(u)).cuda()
+    d_t = torch.empty_like(d_u)
+    rc = _noalloc(lib, d_u.data_ptr(), d_t.data_ptr(), len(u), wrong, stream)
+    torch.cuda.synchronize()
+    assert rc == want_rc, (native.error_string(rc), want_rc)
+    if rc == native.QZGPU_NO_ERROR:
+        assert np.array_equal(d_t.cpu().numpy(), expected)
