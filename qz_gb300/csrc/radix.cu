@@ -12,20 +12,24 @@
 //     not constant in the group; the group runs only those.  Pass 0 needs no
 //     stability (equal keys may leave in any order): tiles rank with shared
 //     atomics and reserve their output with one atomic per digit on the
-//     group's cursor.  The later passes are stable: each tile takes a ticket in
-//     order, publishes its digit counts, and looks back over the tiles before
-//     it in the same group for its exclusive prefix (decoupled look-back), then
-//     scatters through shared memory so that each digit's run leaves as
-//     coalesced writes.  A tile loads its keys to registers and its values to
-//     shared memory (4-byte cp.async) together, and finds its group through
-//     the tile table the histogram kernel writes.
+//     group's cursor; its tiles are fixed per CTA, so each CTA loads its next
+//     tile by bulk copies (on an mbarrier) while it sorts the current one.
+//     The later passes are stable: each tile takes a ticket in order, ranks
+//     its digits per warp (a match on the digit's high four bits and ballots
+//     on the low four), publishes its digit counts, and looks back over the
+//     tiles before it in the same group for its exclusive prefix (decoupled
+//     look-back), then scatters through shared memory so that each digit's run
+//     leaves as coalesced writes.  A stable tile loads its keys to registers
+//     and its values to shared memory (4-byte cp.async) together, and finds
+//     its group through the tile table the histogram kernel writes.
 //
 // Look-back waits are bounded: a tile only waits on tiles that took earlier
 // tickets, which publish their counts before they wait themselves; a wait that
 // exceeds its iteration limit records QZGPU_TIMEOUT in the status word and the
 // tile goes on (its positions stay inside its group), and the kernels whose
 // stores such a failure could misplace return at entry once the status word
-// is set; the host reads it after every round.
+// is set; the host reads it after every round.  A bulk-copy wait that runs out
+// records QZGPU_TIMEOUT too, and its tile stores nothing.
 #include "engine.h"
 #include "radix.cuh"
 #include "scan.cuh"
